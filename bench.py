@@ -1,0 +1,445 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 TDC focus (TdcProcessor::start's hot path).
+
+Workload: the precision study -- 1024 x 1024 pixels at 1 mm, 4096 chirps x 1024
+samples over a 2 m jittered trajectory (FP64 positions and grid), 50 Rayleigh
+targets + noise, seeded synthetic data. Metric: Gcorr/s (pixel x chirp x
+sample correlations per second).
+
+One JSON line on stdout:
+  value     device-resident throughput of the FP32-bulk focus (inputs in HBM)
+  e2e       the same metric through the processor C ABI with host buffers
+            (setRawData / setFocusGrid / start: H2D, focus, D2H every step)
+  roofline  focus kernel vs the measured FP32 FFMA peak (8 FLOP = one complex
+            multiply-accumulate per correlation)
+  cpu_baseline  the FP64 OpenMP oracle loop on the host cores, bounded sample
+  plain     the all-FP64-phase comparator kernel and the speed-up over it
+  accuracy  engine vs the FP64 oracle on a pixel sample (rel. L2, phase, peak)
+
+``--impl reference`` times the reference arm: the reference has no CPU focus,
+so its CPU implementation of the path is the oracle's restatement (port),
+with all host threads, on bounded pixel samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "sarlab-tdc_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Gcorr/s (pixel*chirp*sample) & p50/p99 focus latency vs plain @<=1e-4 L2"
+UNIT = "Gcorr/s"
+FLOP_PER_CORR = 8.0  # complex multiply-accumulate: 4 FFMA
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--side", type=int, default=1024, help="grid side (pixels)")
+    ap.add_argument("--chirps", type=int, default=4096)
+    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--quick", action="store_true", help="skip plain / e2e / CPU legs")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the oracle accuracy check")
+    return ap.parse_args()
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = max((num(r[2]) or 0) for r in rows)
+        power = [num(r[3]) for r in rows if num(r[3]) is not None]
+        loaded = [s for s in sm if s >= 0.5 * smax] or sm
+        reasons = set()
+        names = {5: "hw_slowdown", 6: "hw_thermal_slowdown", 7: "sw_thermal_slowdown", 8: "sw_power_cap"}
+        for r in rows:
+            for i, nm in names.items():
+                if r[i].lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(loaded)) if loaded else None, "sm_max_mhz": smax,
+                "power_w_max": max(power) if power else None, "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+def make_scene(args, device):
+    from sarlabtdc import scenes
+
+    t = time.time()
+    sc = scenes.config2(device=device, n_pix_side=args.side, n_pri=args.chirps, n_samples=args.samples)
+    log(f"scene: {sc.n_pix} px x {sc.n_pri} chirps x {sc.n_samples} samples "
+        f"({sc.correlations() / 1e9:.1f} Gcorr) generated in {time.time() - t:.1f}s")
+    return sc
+
+
+def sample_pixels(sc, n_random, seed=0):
+    rng = np.random.default_rng(seed)
+    flat = sc.grid.reshape(-1, 3)
+    near = [int(np.argmin(np.linalg.norm(flat - t, axis=1))) for t in sc.targets]
+    rnd = rng.choice(flat.shape[0], size=min(n_random, flat.shape[0]), replace=False).tolist()
+    return np.array(sorted(set(near + rnd)), dtype=np.int64)
+
+
+def oracle_problem(sc, api):
+    import oracle
+
+    return oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions,
+                          modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid)
+
+
+def oracle_opts():
+    import oracle
+
+    # Hann is applied to the raw data by the generator: no range window, infinite Doppler band
+    return oracle.Opts(applyRangeWin=False, dopplerBandwidth=float("inf"))
+
+
+def time_oracle(sc, api, budget_s, threads):
+    """FP64 oracle throughput (Gcorr/s) on a bounded pixel sample sized to ~budget_s."""
+    import oracle
+
+    build_oracle()
+    prob = oracle_problem(sc, api)
+    o = oracle_opts()
+    rng = np.random.default_rng(123)
+    per_px = sc.n_pri * sc.n_samples
+    n = 16
+    t = time.perf_counter()
+    oracle.focus(prob, o, pixels=rng.choice(sc.n_pix, n, replace=False), threads=threads)
+    dt = time.perf_counter() - t
+    n2 = int(max(n, min(sc.n_pix, n * budget_s / max(dt, 1e-3))))
+    pix = rng.choice(sc.n_pix, n2, replace=False)
+    t = time.perf_counter()
+    oracle.focus(prob, o, pixels=pix, threads=threads)
+    dt = time.perf_counter() - t
+    return n2 * per_px / dt / 1e9, n2, dt
+
+
+def build_oracle():
+    sys.path.insert(0, str(ROOT))
+    from oracle import build as ob
+
+    ob.build_oracle()
+
+
+def fp32_peak_tflops(lib, torch):
+    import ctypes as C
+
+    dev = torch.cuda.current_device()
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    scratch = torch.empty(n_sm * 64 * 8, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    flops = C.c_double()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc = lib.tdc_probe_fma(0, n_sm * 8, 4000, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert rc == 0
+        best = max(best, flops.value / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    fp64 = 0.0
+    for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.tdc_probe_fma(1, n_sm * 2, 200, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64 = max(fp64, flops.value / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best, fp64, n_sm
+
+
+def load_traffic():
+    f = ROOT / "profiles" / "focus_fp32_traffic.json"
+    if f.exists():
+        try:
+            return json.loads(f.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    import _sarlabtdc
+    import _tdc_capi
+
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    torch.cuda.set_device(0)
+    lib = _tdc_capi.lib()
+    sc = make_scene(args, "cuda")
+    api = sc.api_arrays()
+    P, Cn, S = sc.n_pix, sc.n_pri, sc.n_samples
+    corr = sc.correlations()
+    inf = float("inf")
+    start_args = (0.0, inf, False, False, True)
+
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                 api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+    p.setChirpPositionsF64(sc.positions)
+    p.setFocusGridF64(sc.grid)
+    p.prepare(*start_args)
+    p.uploadGrid()
+    path = p.path()
+    img = torch.empty(P, dtype=torch.complex64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    for _ in range(max(3, args.warmup)):
+        p.focusDevice(img, stream)
+        flush.zero_()
+    p.check(stream)
+
+    clocks = Clocks()
+    clocks.start()
+    time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for e0, e1 in evs:
+        e0.record(stream)
+        p.focusDevice(img, stream)
+        e1.record(stream)
+        flush.zero_()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    p.check(stream)
+    total_ms = t0.elapsed_time(t1)
+    step_ms = np.array([a.elapsed_time(b) for a, b in evs])
+    value = corr * args.steps / (total_ms / 1e3) / 1e9
+    kernel_gcorr = corr / (step_ms.mean() / 1e3) / 1e9
+    log(f"value {value:.1f} Gcorr/s  focus launch {step_ms.mean():.2f} ms  path={path}  clocks={clk}")
+    image = img.cpu().numpy()
+
+    peak_tf, fp64_tf, n_sm = fp32_peak_tflops(lib, torch)
+    achieved_tf = kernel_gcorr * FLOP_PER_CORR / 1e3
+    traffic = load_traffic()
+    roofline = {"bound": "fp32", "achieved": round(achieved_tf, 2), "peak": round(peak_tf, 2), "unit": "TFLOP/s",
+                "frac": round(achieved_tf / peak_tf, 4),
+                "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                "peak_source": "measured FFMA probe (tdc_probe_fma) on this GPU, this run",
+                "flop_per_corr": FLOP_PER_CORR, "fp64_tflops_measured": round(fp64_tf, 3),
+                "kernel": "focus_fp32_kernel"}
+
+    out = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
+           "config": {"workload": f"precision study: {args.side}x{args.side} px @1mm, {Cn} chirps x {S} samples, "
+                                  "2 m jittered rail, FP64 positions + grid",
+                      "pixels": P, "chirps": Cn, "samples": S, "correlations_per_step": corr,
+                      "l2": "256 MiB buffer written between timed steps", "path": path},
+           "latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 3),
+                          "p99": round(float(np.percentile(step_ms, 99)), 3)},
+           "gpu_launches": 2 * args.steps, "clocks": clk, "roofline": roofline}
+
+    if args.no_accuracy:
+        print(json.dumps(out), flush=True)
+        return
+    # accuracy vs the FP64 oracle on a pixel sample (targets + random)
+    import oracle
+
+    build_oracle()
+    pix = sample_pixels(sc, 192)
+    t = time.time()
+    ref = oracle.focus(oracle_problem(sc, api), oracle_opts(), pixels=pix)
+    got = image[pix]
+    sel = np.abs(ref) >= np.abs(ref).max() * 1e-2
+    acc = {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+           "max_phase_rad": float(np.max(np.abs(np.angle(got[sel] * np.conj(ref[sel]))))),
+           "peak_err": float(abs(np.abs(got).max() - np.abs(ref).max()) / np.abs(ref).max()),
+           "pixels": int(pix.size), "oracle": "FP64 on the same inputs"}
+    out["accuracy"] = acc
+    log(f"accuracy {acc} ({time.time() - t:.1f}s)")
+
+    if not args.quick:
+        # plain all-FP64-phase comparator on a row band of the same grid
+        rows = max(8, min(args.side, 64))
+        q = _sarlabtdc.TdcProcessor(0)
+        q.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                     api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+        q.setChirpPositionsF64(sc.positions)
+        band = np.ascontiguousarray(sc.grid[:rows])
+        q.setFocusGridF64(band)
+        q.setPrecision("fp64")
+        q.prepare(*start_args)
+        q.uploadGrid()
+        pimg = torch.empty(q.numPixels(), dtype=torch.complex64, device="cuda")
+        q.focusDevice(pimg, stream)
+        q.check(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        q.focusDevice(pimg, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        q.check(stream)
+        plain_gcorr = band.shape[0] * band.shape[1] * Cn * S / (e0.elapsed_time(e1) / 1e3) / 1e9
+        pim = pimg.cpu().numpy()
+        band_pix = pix[pix < pim.size]
+        plain_acc = None
+        if band_pix.size:
+            rb = oracle.focus(oracle_problem(sc, api), oracle_opts(), pixels=band_pix)
+            plain_acc = float(np.linalg.norm(pim[band_pix] - rb) / np.linalg.norm(rb))
+        out["plain"] = {"value": round(plain_gcorr, 2), "unit": UNIT, "speedup": round(kernel_gcorr / plain_gcorr, 2),
+                        "rows": rows, "rel_l2": plain_acc, "kernel": "focus_fp64_kernel"}
+        log(f"plain {out['plain']}")
+        del q
+
+        # e2e through the processor C ABI with host buffers
+        e2e_steps = max(2, min(args.steps, 3))
+        times, stats = [], None
+        for i in range(1 + e2e_steps):
+            t = time.perf_counter()
+            p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                         api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+            p.setChirpPositionsF64(sc.positions)
+            p.setFocusGridF64(sc.grid)
+            p.start(*start_args)
+            host_img = p.getFocusedImage()
+            dt = time.perf_counter() - t
+            stats = p.lastStats()
+            if i > 0:
+                times.append(dt)
+        e2e_val = corr / float(np.mean(times)) / 1e9
+        out["e2e"] = {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": int(stats["h2d_bytes"]),
+                      "d2h_bytes_per_step": int(stats["d2h_bytes"]), "steps": e2e_steps,
+                      "ms_per_step": round(1e3 * float(np.mean(times)), 2),
+                      "stages_ms": {k: round(stats[k], 3) for k in ("h2d_ms", "prep_ms", "focus_ms", "d2h_ms",
+                                                                      "total_ms")},
+                      "kernel_launches_per_step": stats["kernel_launches"]}
+        assert np.array_equal(host_img.ravel(), image), "e2e image differs from the device-resident image"
+        log(f"e2e {out['e2e']}")
+
+        cpu_g, npx, dt = time_oracle(sc, api, args.cpu_seconds, os.cpu_count())
+        out["cpu_baseline"] = {"value": round(cpu_g, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{npx} random pixels x {Cn} chirps x {S} samples ({dt:.1f}s), "
+                                         "FP64 OpenMP oracle loop"}
+        log(f"cpu {out['cpu_baseline']}")
+    print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import torch
+
+    build_oracle()
+    device = "cuda" if torch.cuda.is_available() else "cpu"
+    sc = make_scene(args, device)
+    api = sc.api_arrays()
+    cores = os.cpu_count()
+    import oracle
+
+    prob = oracle_problem(sc, api)
+    o = oracle_opts()
+    rng = np.random.default_rng(99)
+    per_px = sc.n_pri * sc.n_samples
+    # size one step to ~budget seconds of CPU work
+    t = time.perf_counter()
+    oracle.focus(prob, o, pixels=rng.choice(sc.n_pix, 8, replace=False), threads=cores)
+    dt = time.perf_counter() - t
+    budget = max(2.0, min(15.0, 100.0 / max(1, args.steps + args.warmup)))
+    npx = int(max(8, min(sc.n_pix, 8 * budget / max(dt, 1e-3))))
+    for _ in range(args.warmup):
+        oracle.focus(prob, o, pixels=rng.choice(sc.n_pix, max(8, npx // 8), replace=False), threads=cores)
+    times = []
+    for _ in range(args.steps):
+        pix = rng.choice(sc.n_pix, npx, replace=False)
+        t = time.perf_counter()
+        oracle.focus(prob, o, pixels=pix, threads=cores)
+        times.append(time.perf_counter() - t)
+    value = npx * per_px / float(np.mean(times)) / 1e9
+    out = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(times)), 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+           "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
+           "config": {"workload": f"precision study: {args.side}x{args.side} px @1mm, {sc.n_pri} chirps x "
+                                  f"{sc.n_samples} samples, 2 m jittered rail, FP64 positions + grid",
+                      "pixels": sc.n_pix, "chirps": sc.n_pri, "samples": sc.n_samples},
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{npx} random pixels per step x {sc.n_pri} chirps x {sc.n_samples} samples; "
+                                      "the reference has no CPU focus path: FP64 OpenMP restatement of "
+                                      "tdckernels.cu:70-315 (oracle/)"},
+           "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.gpus != 1 and args.impl == "ours":
+        print(json.dumps({"error": "this engine runs one process on one GPU; run with --gpus 1"}))
+        return 2
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

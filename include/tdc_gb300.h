@@ -1,0 +1,196 @@
+/*
+ * tdc_gb300.h -- C ABI of the GB300 time-domain-correlation (TDC) focus engine.
+ *
+ * Two layers:
+ *
+ *  1. The processor API: one function per public method of the sarlab-tdc
+ *     class `TdcProcessor` (tdc-lib/include/tdcprocessor.h:42-135), which is
+ *     what the reference's pybind module `_sarlabtdc`
+ *     (py-sarlabtdc/src/interface.cpp:15-22) binds. Same argument meaning,
+ *     same ownership rules (inputs are borrowed host pointers read during
+ *     tdc_processor_start; the image buffer belongs to the processor), and the
+ *     same error classes, returned as status codes instead of C++ exceptions.
+ *
+ *  2. The device seam: functions on device pointers that replace the kernel
+ *     wrappers of tdc-lib/include/tdckernels.h:20-97 (initRangeWindow,
+ *     createWindow, referenceResponse, correlateAndSum, sumScratchSize). The
+ *     per-pixel, per-chunk launch sequence of the reference becomes one fused
+ *     launch over all pixels and chirps.
+ *
+ * All functions return TDC_OK (0) or a negative tdc_status; tdc_last_error()
+ * gives a message for the calling thread's most recent failure. No C++
+ * exception crosses this boundary. Streams are passed as void* (a cudaStream_t;
+ * NULL is the legacy default stream).
+ */
+#ifndef TDC_GB300_H
+#define TDC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDC_GB300_ABI_VERSION 1
+
+typedef enum tdc_status {
+    TDC_OK = 0,
+    TDC_ERR_INVALID_ARGUMENT = -1, /* std::invalid_argument in the reference (tdcprocessor.cpp:189-195) */
+    TDC_ERR_CUDA = -2,             /* std::runtime_error from a CUDA failure (tdcprocessor.cpp:50-53,149-154) */
+    TDC_ERR_STATE = -3,            /* call order violated (start before setRawData / setFocusGrid) */
+    TDC_ERR_NO_MEMORY = -4,        /* device or pinned host allocation failed */
+    TDC_ERR_TIMEOUT = -5,          /* a kernel's bounded wait expired; the kernel returned early */
+    TDC_ERR_UNSUPPORTED = -6,      /* input outside what this build handles (message says which) */
+    TDC_ERR_SHAPE = -7             /* array shape mismatch (runtime_error in the pybind wrapper) */
+} tdc_status;
+
+/* Message for the calling thread's most recent failure ("" if none). */
+const char *tdc_last_error(void);
+int tdc_abi_version(void);
+
+/* ======================================================================== */
+/* 1. Processor API (replaces class TdcProcessor, tdcprocessor.h:42-135).   */
+/* ======================================================================== */
+
+typedef struct tdc_processor tdc_processor;
+
+/* TdcProcessor(int gpuNum) -- tdcprocessor.cpp:39-55 (cudaSetDevice). */
+int tdc_processor_create(int gpu_num, tdc_processor **out);
+/* ~TdcProcessor() */
+int tdc_processor_destroy(tdc_processor *proc);
+
+/*
+ * TdcProcessor::setRawData -- tdcprocessor.h:104-107, tdcprocessor.cpp:169-209.
+ * raw_iq:       nPri x nSamples complex float (interleaved I/Q), row-major
+ * pri_times:    nPri floats (stored, unused by the focus, as in the reference)
+ * sample_times: nSamples floats, seconds from the PRI start
+ * position:     nPri x nSamples x 3 floats (x, y, z), metres
+ * velocity:     nPri x nSamples x 3 floats
+ * attitude:     nPri x nSamples x 4 floats, body->local quaternion (a, b, c, d)
+ * body_boresight: 3 floats
+ * The pointers are borrowed: they must stay valid until the next start()
+ * returns. Errors: TDC_ERR_INVALID_ARGUMENT when n_pri <= 0 or n_samples <= 0.
+ */
+int tdc_processor_set_raw_data(tdc_processor *proc, const float *raw_iq, const float *pri_times,
+                               const float *sample_times, const float *position, const float *velocity,
+                               const float *attitude, int n_pri, int n_samples, float mod_rate,
+                               float start_freq, const float *body_boresight);
+
+/* TdcProcessor::setFocusGrid -- tdcprocessor.h:121, tdcprocessor.cpp:211-217.
+ * focus_grid: n_rows x n_cols x 3 floats (x, y, z), borrowed until start() returns. */
+int tdc_processor_set_focus_grid(tdc_processor *proc, const float *focus_grid, int n_rows, int n_cols);
+
+/*
+ * TdcProcessor::start -- tdcprocessor.h:67-68, tdcprocessor.cpp:59-167.
+ * Blocking. Windows, forms the reference response and correlates every pixel
+ * against every chirp on the GPU, then copies the image to the host buffer.
+ */
+int tdc_processor_start(tdc_processor *proc, float doppler_win_center, float doppler_bandwidth,
+                        int dop_centroid_win, int apply_range_win, int doppler_win_taper);
+
+/* TdcProcessor::imageBuffer -- tdcprocessor.cpp:240-243. n_rows x n_cols complex
+ * float (interleaved), owned by the processor, valid until the next start() or
+ * destroy. NULL before the first start(). */
+const float *tdc_processor_image_buffer(const tdc_processor *proc);
+
+/* Focus-grid shape last set (getFocusedImage uses it, tdcprocessor_wrapper.cpp:155-163). */
+int tdc_processor_grid_shape(const tdc_processor *proc, int *n_rows, int *n_cols);
+
+/* ---- extensions (no reference counterpart) ---- */
+
+/* Per-chirp antenna positions in FP64 (n_pri x 3), overriding the FP32
+ * per-sample positions of setRawData for the range/phase computation. Needed
+ * where FP32 rounding of metre-scale coordinates is itself above the phase
+ * tolerance. Borrowed like the other inputs. NULL clears the override. */
+int tdc_processor_set_chirp_positions_f64(tdc_processor *proc, const double *position_f64, int n_pri);
+
+/* FP64 focus grid (n_rows x n_cols x 3), used instead of the FP32 grid. */
+int tdc_processor_set_focus_grid_f64(tdc_processor *proc, const double *focus_grid, int n_rows, int n_cols);
+
+typedef enum tdc_precision {
+    TDC_PRECISION_FP32_BULK = 0, /* double-float range/phase per (pixel, chirp), FP32 phasors + MAC */
+    TDC_PRECISION_FP64_PHASE = 1 /* plain comparator: FP64 phase per sample, FP32 MAC */
+} tdc_precision;
+
+int tdc_processor_set_precision(tdc_processor *proc, int precision);
+
+typedef struct tdc_start_stats {
+    double h2d_ms;        /* host->device copies of the inputs */
+    double prep_ms;       /* windowing of raw chirps + trajectory records */
+    double focus_ms;      /* the fused correlate-sum launch(es) */
+    double d2h_ms;        /* image copy back */
+    double total_ms;      /* wall time of start() */
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+    int64_t correlations; /* pixels x chirps x samples */
+    int path;             /* tdc_path used */
+    int kernel_launches;  /* launches of this library's kernels inside start() */
+} tdc_start_stats;
+
+typedef enum tdc_path {
+    TDC_PATH_FP32_BULK = 0,    /* per-chirp trajectory, uniform sample spacing */
+    TDC_PATH_FP64_PHASE = 1,   /* comparator, per-chirp trajectory */
+    TDC_PATH_GENERAL = 2       /* per-sample trajectory or non-uniform sample times */
+} tdc_path;
+
+int tdc_processor_last_stats(const tdc_processor *proc, tdc_start_stats *out);
+
+/* ======================================================================== */
+/* 2. Device seam (replaces tdckernels.h:20-97).                            */
+/* ======================================================================== */
+
+/* initRangeWindow (tdckernels.h:20): w[n] = a - (1-a) cos(2 pi n / N), a = 25/46
+ * (Hamming, periodic), or all ones. Device pointer, n_samples floats. */
+int tdc_range_window(float *w_dev, int n_samples, int apply_range_win, void *stream);
+
+/* Skip test of tdcprocessor.cpp:347-383 on (1, default) or off. Takes effect
+ * at the next start() / prepare(). */
+int tdc_processor_set_skip_test(tdc_processor *proc, int enable);
+
+/*
+ * The parts of start() before the per-pixel work, leaving the acquisition
+ * resident in device memory: copy of the raw chirps, range window applied
+ * once per chirp (replacing createWindow's per-pixel range window),
+ * trajectory records and skip-test points (replacing the per-chunk staging
+ * of tdcprocessor.cpp:310-345). Same arguments as start(). Blocking.
+ */
+int tdc_processor_prepare(tdc_processor *proc, float doppler_win_center, float doppler_bandwidth,
+                          int dop_centroid_win, int apply_range_win, int doppler_win_taper);
+
+/* Copy the focus grid set by setFocusGrid / setFocusGrid_f64 to the device. Blocking. */
+int tdc_processor_upload_grid(tdc_processor *proc);
+
+/*
+ * The fused focus (replaces the per-pixel createWindow + referenceResponse +
+ * correlateAndSum launches of tdcprocessor.cpp:82-144, and sumScratchSize):
+ * image_dev[p] (complex float, interleaved) for every pixel of the resident
+ * grid, from the resident acquisition. Asynchronous on `stream` (NULL = the
+ * processor's stream); the processor owns the scratch memory. Call
+ * tdc_processor_check before reading results to collect device-side errors.
+ */
+int tdc_processor_focus_device(tdc_processor *proc, float *image_dev, void *stream);
+
+/* Synchronise `stream` (NULL = the processor's) and report a kernel-side error
+ * (TDC_ERR_TIMEOUT when a bounded wait expired). */
+int tdc_processor_check(tdc_processor *proc, void *stream);
+
+/* Number of pixels of the resident grid. */
+int tdc_processor_num_pixels(const tdc_processor *proc, int64_t *n_pix);
+
+/* tdc_path the next focus will take, or -1 when nothing is resident. */
+int tdc_processor_path(const tdc_processor *proc);
+
+/* ---- measurement helper (no reference counterpart) ---- */
+
+/* FMA throughput probe: blocks x 256 threads x iters x 16 FMAs, FP32 (fp64 = 0)
+ * or FP64. *flops receives the FLOP count (2 per FMA); the caller times the
+ * launch with events on `stream`. scratch_dev: >= blocks x 8 bytes (never written
+ * in practice). */
+int tdc_probe_fma(int fp64, int blocks, int iters, void *scratch_dev, double *flops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDC_GB300_H */

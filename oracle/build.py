@@ -1,0 +1,83 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+* ``oracle/_build/libtdc_oracle.so`` -- the FP64 C restatement in
+  ``oracle/tdc_oracle.c`` (gcc -O2 -fopenmp).
+* ``oracle/_ref/libtdc_refmath.so`` -- the reference's own host-side math
+  (``tdc-lib/include/gpumath.h`` and ``windowing.h``, compiled from where they
+  lie in the reference checkout by g++, through ``oracle/ref_math_shim.cpp``).
+  Built only when the reference checkout is present (``TDC_REFERENCE_ROOT`` or
+  ``/root/reference``); it is used to pin the oracle's window and quaternion
+  math to the reference's, never by the product.
+
+Both outputs are git-ignored build products.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+ORACLE_SO = BUILD / "libtdc_oracle.so"
+REFMATH_SO = REF_OUT / "libtdc_refmath.so"
+
+
+def reference_root() -> Path | None:
+    root = Path(os.environ.get("TDC_REFERENCE_ROOT", "/root/reference"))
+    inc = root / "tdc-lib" / "include"
+    if (inc / "gpumath.h").is_file() and (inc / "windowing.h").is_file():
+        return root
+    return None
+
+
+def _stale(out: Path, srcs: list[Path]) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(s.stat().st_mtime > t for s in srcs)
+
+
+def build_oracle(force: bool = False) -> Path:
+    src = HERE / "tdc_oracle.c"
+    if force or _stale(ORACLE_SO, [src, Path(__file__)]):
+        BUILD.mkdir(exist_ok=True)
+        tmp = ORACLE_SO.with_suffix(".so.tmp%d" % os.getpid())
+        cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-Wall",
+               "-o", str(tmp), str(src), "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_refmath(force: bool = False) -> Path | None:
+    root = reference_root()
+    if root is None:
+        return REFMATH_SO if REFMATH_SO.exists() else None
+    inc = root / "tdc-lib" / "include"
+    shim = HERE / "ref_math_shim.cpp"
+    srcs = [shim, inc / "gpumath.h", inc / "windowing.h", inc / "tuning.h", Path(__file__)]
+    if force or _stale(REFMATH_SO, srcs):
+        REF_OUT.mkdir(exist_ok=True)
+        cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+        tmp = REFMATH_SO.with_suffix(".so.tmp%d" % os.getpid())
+        # -ffp-contract=off: the host build of the reference math does plain
+        # IEEE float operations, no fused multiply-adds.
+        cmd = ["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off",
+               "-I", str(inc), "-I", str(cuda_inc), "-o", str(tmp), str(shim)]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, REFMATH_SO)
+    return REFMATH_SO
+
+
+def main(argv: list[str]) -> int:
+    force = "--force" in argv
+    print(build_oracle(force))
+    print(build_refmath(force))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))

@@ -1,0 +1,190 @@
+"""``_sarlabtdc`` -- the GB300 engine behind the reference's Python module interface.
+
+Mirrors the pybind11 module of py-sarlabtdc (py-sarlabtdc/src/interface.cpp:9-22,
+py-sarlabtdc/src/tdcprocessor_wrapper.cpp:19-170): class ``TdcProcessor(gpuNum)``
+with ``setRawData``, ``setFocusGrid``, ``start`` and ``getFocusedImage``, the same
+positional arguments, the same numpy conversions (any numeric array is cast to
+C-contiguous complex64 / float32, like ``py::array_t<T, c_style>``), the same
+shape checks and messages (RuntimeError), ValueError for ``nPri``/``nSamples`` <= 0,
+and references kept to the arrays until they are replaced (the processor
+borrows their memory, tdcprocessor.cpp:176-186). The calls go through the C ABI
+of ``libtdc_gb300.so``; everything else in this class is additive.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+import _tdc_capi as _lib
+
+__doc__ = "Time-domain correlation SAR processor for high bandwidth mmWave radars."
+
+
+def _arr(x, dtype):
+    return np.ascontiguousarray(np.asarray(x).astype(dtype, copy=False))
+
+
+class TdcProcessor:
+    """Time-domain correlation SAR processor (tdc-lib/include/tdcprocessor.h:42-200)."""
+
+    def __init__(self, gpuNum: int):
+        L = _lib.lib()
+        h = C.c_void_p()
+        _lib.check(L.tdc_processor_create(int(gpuNum), C.byref(h)))
+        self._h = h
+        self._raw_refs = ()
+        self._grid_ref = None
+        self._pos64_ref = None
+        self._grid_rows = 0
+        self._grid_cols = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().tdc_processor_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---- reference methods -------------------------------------------------
+
+    def start(self, dopplerWinCenter, dopplerBandwidth, dopCentroidWin, applyRangeWin, dopplerWinTaper=True):
+        """Run the focus (tdcprocessor.h:67-68). Blocks until the image is on the host."""
+        _lib.check(_lib.lib().tdc_processor_start(self._h, float(dopplerWinCenter), float(dopplerBandwidth),
+                                                  int(bool(dopCentroidWin)), int(bool(applyRangeWin)),
+                                                  int(bool(dopplerWinTaper))))
+
+    def setRawData(self, rawData, priTimes, sampleTimes, position, velocity, attitude, modRate, startFreq,
+                   bodyBoresight, /):
+        """tdcprocessor_wrapper.cpp:27-126: ndim checks, then shape checks, then setRawData."""
+        raw = _arr(rawData, np.complex64)
+        pri = _arr(priTimes, np.float32)
+        st = _arr(sampleTimes, np.float32)
+        pos = _arr(position, np.float32)
+        vel = _arr(velocity, np.float32)
+        att = _arr(attitude, np.float32)
+        bore = _arr(bodyBoresight, np.float32)
+        if raw.ndim != 2:
+            raise RuntimeError("rawData must be 2D")
+        if pri.ndim != 1:
+            raise RuntimeError("priTimes must be 1D")
+        if st.ndim != 1:
+            raise RuntimeError("sampleTimes must be 1D")
+        if pos.ndim != 3:
+            raise RuntimeError("position must be 3D")
+        if vel.ndim != 3:
+            raise RuntimeError("velocity must be 3D")
+        if att.ndim != 3:
+            raise RuntimeError("attitude must be 3D")
+        if bore.ndim != 1:
+            raise RuntimeError("bodyBoresight must be 1D")
+        n_pri, n_samples = raw.shape
+        if pri.shape[0] != n_pri:
+            raise RuntimeError("priTimes shape is incorrect")
+        if st.shape[0] != n_samples:
+            raise RuntimeError("sampleTimes shape is incorrect")
+        if pos.shape != (n_pri, n_samples, 3):
+            raise RuntimeError("position shape is incorrect")
+        if vel.shape != (n_pri, n_samples, 3):
+            raise RuntimeError("velocity shape is incorrect")
+        if att.shape != (n_pri, n_samples, 4):
+            raise RuntimeError("attitude shape is incorrect")
+        if bore.shape[0] != 3:
+            raise RuntimeError("bodyBoresight shape is incorrect")
+        self._raw_refs = (raw, pri, st, pos, vel, att, bore)
+        self._pos64_ref = None
+        p = _lib.ptr
+        _lib.check(_lib.lib().tdc_processor_set_raw_data(
+            self._h, p(raw), p(pri), p(st), p(pos), p(vel), p(att), int(n_pri), int(n_samples),
+            float(modRate), float(startFreq), p(bore)))
+
+    def setFocusGrid(self, focusGrid, /):
+        """tdcprocessor_wrapper.cpp:129-153."""
+        grid = _arr(focusGrid, np.float32)
+        if grid.ndim != 3:
+            raise RuntimeError("focusGrid must be 3D")
+        rows, cols = grid.shape[0], grid.shape[1]
+        if grid.shape[2] != 3:
+            raise RuntimeError("focusGrid shape is incorrect")
+        self._grid_ref = grid
+        self._grid_rows, self._grid_cols = rows, cols
+        _lib.check(_lib.lib().tdc_processor_set_focus_grid(self._h, _lib.ptr(grid), int(rows), int(cols)))
+
+    def getFocusedImage(self):
+        """tdcprocessor_wrapper.cpp:155-163: a new complex64 [rows, cols] copy of the image."""
+        rows, cols = self._grid_rows, self._grid_cols
+        addr = _lib.lib().tdc_processor_image_buffer(self._h)
+        out = np.empty((rows, cols), dtype=np.complex64)
+        if addr and rows * cols:
+            C.memmove(out.ctypes.data, addr, rows * cols * 8)
+        elif rows * cols:
+            out[...] = 0  # the reference copies from a buffer that does not exist yet; we return zeros
+        return out
+
+    # ---- extensions (no reference counterpart) ------------------------------
+
+    def setChirpPositionsF64(self, position):
+        """Per-chirp FP64 antenna positions [nPri, 3] used for range and phase."""
+        pos = np.ascontiguousarray(np.asarray(position, dtype=np.float64))
+        if pos.ndim != 2 or pos.shape[1] != 3:
+            raise RuntimeError("position shape is incorrect")
+        self._pos64_ref = pos
+        _lib.check(_lib.lib().tdc_processor_set_chirp_positions_f64(self._h, _lib.ptr(pos), int(pos.shape[0])))
+
+    def setFocusGridF64(self, focusGrid):
+        grid = np.ascontiguousarray(np.asarray(focusGrid, dtype=np.float64))
+        if grid.ndim != 3:
+            raise RuntimeError("focusGrid must be 3D")
+        if grid.shape[2] != 3:
+            raise RuntimeError("focusGrid shape is incorrect")
+        self._grid_ref = grid
+        self._grid_rows, self._grid_cols = grid.shape[0], grid.shape[1]
+        _lib.check(_lib.lib().tdc_processor_set_focus_grid_f64(self._h, _lib.ptr(grid), int(grid.shape[0]),
+                                                               int(grid.shape[1])))
+
+    def setPrecision(self, precision: str):
+        """'fp32' (double-float range/phase, FP32 bulk; default) or 'fp64' (plain FP64-phase comparator)."""
+        code = {"fp32": _lib.PRECISION_FP32_BULK, "fp64": _lib.PRECISION_FP64_PHASE}[precision]
+        _lib.check(_lib.lib().tdc_processor_set_precision(self._h, code))
+
+    def setSkipTest(self, enable: bool):
+        _lib.check(_lib.lib().tdc_processor_set_skip_test(self._h, int(bool(enable))))
+
+    def lastStats(self) -> dict:
+        s = _lib.StartStats()
+        _lib.check(_lib.lib().tdc_processor_last_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    # device-resident use (torch tensors or raw device addresses)
+    def prepare(self, dopplerWinCenter, dopplerBandwidth, dopCentroidWin, applyRangeWin, dopplerWinTaper=True):
+        _lib.check(_lib.lib().tdc_processor_prepare(self._h, float(dopplerWinCenter), float(dopplerBandwidth),
+                                                    int(bool(dopCentroidWin)), int(bool(applyRangeWin)),
+                                                    int(bool(dopplerWinTaper))))
+
+    def uploadGrid(self):
+        _lib.check(_lib.lib().tdc_processor_upload_grid(self._h))
+
+    def numPixels(self) -> int:
+        n = C.c_int64()
+        _lib.check(_lib.lib().tdc_processor_num_pixels(self._h, C.byref(n)))
+        return n.value
+
+    def path(self) -> str:
+        return _lib.PATH_NAMES.get(_lib.lib().tdc_processor_path(self._h), "none")
+
+    def focusDevice(self, image, stream=None):
+        """Focus the resident acquisition onto the resident grid into ``image``
+        (a complex64 CUDA tensor of numPixels() elements, or a device address)."""
+        addr = image if isinstance(image, int) else image.data_ptr()
+        st = None
+        if stream is not None:
+            st = stream if isinstance(stream, int) else stream.cuda_stream
+        _lib.check(_lib.lib().tdc_processor_focus_device(self._h, addr, st))
+
+    def check(self, stream=None):
+        st = None
+        if stream is not None:
+            st = stream if isinstance(stream, int) else stream.cuda_stream
+        _lib.check(_lib.lib().tdc_processor_check(self._h, st))

@@ -1,0 +1,901 @@
+// tdc_capi.cpp -- host side of the GB300 TDC engine behind the C ABI of
+// include/tdc_gb300.h: the processor (TdcProcessor's contract,
+// tdc-lib/src/tdcprocessor.cpp:39-243), input analysis, the device-resident
+// acquisition, work planning and kernel launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "tdc_gb300.h"
+#include "tdc_internal.h"
+
+using namespace tdc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? TDC_ERR_NO_MEMORY : TDC_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define TDC_CK(call, what)                           \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        else p = nullptr;
+        return e;
+    }
+    template <class T>
+    T *as() const
+    {
+        return static_cast<T *>(p);
+    }
+};
+
+// Grow-only pinned host buffer.
+struct PinnedBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMallocHost(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        else p = nullptr;
+        return e;
+    }
+};
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---- host FP32 math with the reference's semantics (gpumath.h, windowing.h) ----
+// Quaternions (a, b, c, d) = (w, x, y, z).
+void q_prod_f(const float *a, const float *b, float *o)
+{
+    const float r0 = (a[0] * b[0]) - (a[1] * b[1]) - (a[2] * b[2]) - (a[3] * b[3]);
+    const float r1 = (a[0] * b[1]) + (a[1] * b[0]) + (a[2] * b[3]) - (a[3] * b[2]);
+    const float r2 = (a[0] * b[2]) - (a[1] * b[3]) + (a[2] * b[0]) + (a[3] * b[1]);
+    const float r3 = (a[0] * b[3]) + (a[1] * b[2]) - (a[2] * b[1]) + (a[3] * b[0]);
+    o[0] = r0;
+    o[1] = r1;
+    o[2] = r2;
+    o[3] = r3;
+}
+
+void q_rot_f(const float *q, const float *v, float *o)
+{
+    const float vq[4] = {0.f, v[0], v[1], v[2]};
+    const float qc[4] = {q[0], -q[1], -q[2], -q[3]};
+    float t[4], r[4];
+    q_prod_f(q, vq, t);
+    q_prod_f(t, qc, r);
+    o[0] = r[1];
+    o[1] = r[2];
+    o[2] = r[3];
+}
+
+// Doppler window centre of one trajectory sample (tdckernels.cu:114-122).
+float window_centre(const float *vel, const float *att, const float *bore, float lambda, bool centroid,
+                    float fixed_centre)
+{
+    if (!centroid) return fixed_centre;
+    float ant[3];
+    q_rot_f(att, bore, ant);
+    return 2.0f / lambda * ((vel[0] * ant[0]) + (vel[1] * ant[1]) + (vel[2] * ant[2]));
+}
+
+struct StartOpts {
+    float center = 0.f;
+    float bw = 0.f;
+    int centroid = 0;
+    int range_win = 1;
+    int taper = 1;
+    int skip_test = 1;
+};
+
+void split_dd(double v, float &h, float &l)
+{
+    h = static_cast<float>(v);
+    l = static_cast<float>(v - static_cast<double>(h));
+}
+
+// Phase tolerance for treating the sample frequencies as affine in the sample index.
+constexpr double kUniformPhaseTolRad = 1e-4;
+
+}  // namespace
+
+// ===========================================================================
+// Processor
+// ===========================================================================
+
+struct tdc_processor {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+
+    // Borrowed inputs (setRawData / setFocusGrid).
+    const float *raw = nullptr;
+    const float *pri_times = nullptr;
+    const float *sample_times = nullptr;
+    const float *pos = nullptr;
+    const float *vel = nullptr;
+    const float *att = nullptr;
+    const double *pos64 = nullptr;
+    int C = 0, S = 0;
+    float mod_rate = 0.f, start_freq = 0.f;
+    float bore[3] = {0.f, 0.f, 0.f};
+    float lambda = 0.f;
+    bool has_raw = false;
+
+    const float *grid = nullptr;
+    const double *grid64 = nullptr;
+    int rows = 0, cols = 0;
+    bool has_grid = false;
+
+    int precision = TDC_PRECISION_FP32_BULK;
+    int skip_test = 1;
+
+    // Prepared acquisition (device resident).
+    bool prepared = false;
+    StartOpts opts;
+    bool per_chirp = true;
+    double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
+    double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
+    int s_pad = 0, n_chunks = 0;
+    DevBuf xw, chirps, skip, gs, pos_base, wr, offsets;
+
+    // Device grid.
+    long long P = 0;
+    bool grid_lo_valid = false;
+    double grid_min[3] = {0, 0, 0}, grid_max[3] = {0, 0, 0};
+    DevBuf grid_stage, grid_hi, grid_lo;
+
+    // Focus plan cache + scratch.
+    DevBuf scratch;
+    std::vector<FocusUnit> units_host;
+    long long plan_P = -1;
+    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0;
+    bool plan_uploaded = false;
+
+    DevBuf image_dev;
+    PinnedBuf image_host;
+    bool image_valid = false;
+
+    tdc_start_stats stats{};
+};
+
+namespace {
+
+int check_proc(const tdc_processor *p)
+{
+    if (!p) return fail(TDC_ERR_INVALID_ARGUMENT, "null processor");
+    return TDC_OK;
+}
+
+// Trajectory constant within every chirp (bitwise), per array.
+bool rows_constant(const float *a, int C, int S, int k)
+{
+    if (!a) return true;
+    for (int c = 0; c < C; ++c) {
+        const float *row = a + (size_t)c * S * k;
+        for (int s = 1; s < S; ++s) {
+            if (std::memcmp(row, row + (size_t)s * k, sizeof(float) * k) != 0) return false;
+        }
+    }
+    return true;
+}
+
+// Least-squares affine fit f_s ~ F0 + F1 s of f_s = f0 + K t_s (FP64 on the FP32 inputs).
+void fit_frequencies(const float *t, int S, float f0, float K, double &F0, double &F1, double &resid)
+{
+    std::vector<double> f(S);
+    for (int s = 0; s < S; ++s) f[s] = (double)f0 + (double)K * (double)t[s];
+    if (S == 1) {
+        F0 = f[0];
+        F1 = 0.0;
+        resid = 0.0;
+        return;
+    }
+    const double sm = 0.5 * (S - 1);
+    double fm = 0.0;
+    for (int s = 0; s < S; ++s) fm += f[s];
+    fm /= S;
+    double num = 0.0, den = 0.0;
+    for (int s = 0; s < S; ++s) {
+        num += (s - sm) * (f[s] - fm);
+        den += (s - sm) * (s - sm);
+    }
+    F1 = num / den;
+    F0 = fm - F1 * sm;
+    resid = 0.0;
+    for (int s = 0; s < S; ++s) resid = std::max(resid, std::fabs(f[s] - (F0 + F1 * s)));
+}
+
+double max_range(const double *amin, const double *amax, const double *gmin, const double *gmax)
+{
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        const double d = std::max(std::fabs(amax[k] - gmin[k]), std::fabs(gmax[k] - amin[k]));
+        r2 += d * d;
+    }
+    return std::sqrt(r2);
+}
+
+void stats_reset(tdc_processor *p) { std::memset(&p->stats, 0, sizeof(p->stats)); }
+
+// Upload + prepare the acquisition for the given start() options.
+int prepare(tdc_processor *p, const StartOpts &o, int &launches)
+{
+    if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called before start()");
+    const int C = p->C, S = p->S;
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+
+    // ---- host analysis ----
+    p->per_chirp = (p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
+                   rows_constant(p->att, C, S, 4);
+    fit_frequencies(p->sample_times, S, p->start_freq, p->mod_rate, p->F0, p->F1, p->resid_hz);
+    for (int k = 0; k < 3; ++k) {
+        p->ant_min[k] = std::numeric_limits<double>::infinity();
+        p->ant_max[k] = -std::numeric_limits<double>::infinity();
+    }
+    std::vector<double> base((size_t)C * 3);
+    for (int c = 0; c < C; ++c) {
+        for (int k = 0; k < 3; ++k) {
+            const double v = p->pos64 ? p->pos64[3 * (size_t)c + k] : (double)p->pos[(size_t)c * S * 3 + k];
+            base[3 * (size_t)c + k] = v;
+            p->ant_min[k] = std::min(p->ant_min[k], v);
+            p->ant_max[k] = std::max(p->ant_max[k], v);
+        }
+    }
+    if (!p->per_chirp && p->pos && !p->pos64) {
+        for (size_t i = 0; i < (size_t)C * S; ++i)
+            for (int k = 0; k < 3; ++k) {
+                p->ant_min[k] = std::min(p->ant_min[k], (double)p->pos[3 * i + k]);
+                p->ant_max[k] = std::max(p->ant_max[k], (double)p->pos[3 * i + k]);
+            }
+    }
+
+    // ---- trajectory records (per chirp, or per sample for the general path) ----
+    static const float kZero3[3] = {0.f, 0.f, 0.f};
+    static const float kQId[4] = {1.f, 0.f, 0.f, 0.f};
+    const size_t n_rec = p->per_chirp ? (size_t)C : (size_t)C * S;
+    std::vector<ChirpRec> recs(n_rec);
+    for (int c = 0; c < C; ++c) {
+        const int ns = p->per_chirp ? 1 : S;
+        for (int s = 0; s < ns; ++s) {
+            const size_t e = (size_t)c * S + s;
+            const float *vl = p->vel ? p->vel + 3 * e : kZero3;
+            const float *at = p->att ? p->att + 4 * e : kQId;
+            const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
+            ChirpRec r;
+            float h[3], l[3];
+            for (int k = 0; k < 3; ++k) {
+                if (p->pos64) {
+                    split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
+                } else {
+                    h[k] = p->pos[3 * e + k];
+                    l[k] = 0.f;
+                }
+            }
+            r.p_hi = make_float4(h[0], h[1], h[2], fdc);
+            r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
+            r.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
+            recs[p->per_chirp ? (size_t)c : e] = r;
+        }
+    }
+
+    // ---- skip-test points (tdcprocessor.cpp:347-383, stale staging rows included) ----
+    const int n_chunks = (C + kChunk - 1) / kChunk;
+    std::vector<SkipPoint> skip((size_t)n_chunks * 9);
+    {
+        int rows[3], samples[3];
+        for (int i = 0; i < 3; ++i) {
+            rows[i] = std::max(i * (kChunk / 2) - 1, 0);
+            samples[i] = std::max(i * (S / 2) - 1, 0);
+        }
+        for (int k = 0; k < n_chunks; ++k) {
+            const long base_pri = (long)k * kChunk;
+            const long valid = std::min<long>(kChunk, C - base_pri);
+            for (int i = 0; i < 3; ++i) {
+                long pri;
+                if (rows[i] < valid) pri = base_pri + rows[i];
+                else if (k == 0) pri = -1;  // never-written staging row: zeros
+                else pri = base_pri - kChunk + rows[i];
+                for (int j = 0; j < 3; ++j) {
+                    SkipPoint sp;
+                    if (pri < 0) {
+                        const float zq[4] = {0.f, 0.f, 0.f, 0.f};
+                        const float fdc = window_centre(kZero3, zq, p->bore, p->lambda, o.centroid != 0, o.center);
+                        sp.pos_fdc = make_float4(0.f, 0.f, 0.f, fdc);
+                        sp.vel = make_float4(0.f, 0.f, 0.f, 0.f);
+                    } else {
+                        const size_t e = (size_t)pri * S + samples[j];
+                        const float *ps = p->pos + 3 * e;
+                        const float *vl = p->vel ? p->vel + 3 * e : kZero3;
+                        const float *at = p->att ? p->att + 4 * e : kQId;
+                        const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
+                        sp.pos_fdc = make_float4(ps[0], ps[1], ps[2], fdc);
+                        sp.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
+                    }
+                    skip[(size_t)k * 9 + i * 3 + j] = sp;
+                }
+            }
+        }
+    }
+
+    // ---- per-sample 2 f_s / c0 table (FP64 kernels) ----
+    std::vector<double> gs(S);
+    for (int s = 0; s < S; ++s)
+        gs[s] = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
+
+    // ---- device buffers ----
+    const int s_pad = (int)round_up((size_t)S, kSampleAlign);
+    p->s_pad = s_pad;
+    p->n_chunks = n_chunks;
+    cudaStream_t st = p->stream;
+    TDC_CK(p->xw.ensure((size_t)C * s_pad * 8), "alloc samples");
+    TDC_CK(p->wr.ensure((size_t)S * 4), "alloc range window");
+    TDC_CK(p->chirps.ensure(n_rec * sizeof(ChirpRec)), "alloc chirp records");
+    TDC_CK(p->skip.ensure(skip.size() * sizeof(SkipPoint)), "alloc skip table");
+    TDC_CK(p->gs.ensure((size_t)S * 8), "alloc frequency table");
+    TDC_CK(p->pos_base.ensure((size_t)C * 3 * 8), "alloc base positions");
+
+    TDC_CK(cudaMemcpy2DAsync(p->xw.p, (size_t)s_pad * 8, p->raw, (size_t)S * 8, (size_t)S * 8, C,
+                             cudaMemcpyHostToDevice, st),
+           "copy raw data");
+    TDC_CK(cudaMemcpyAsync(p->chirps.p, recs.data(), n_rec * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
+           "copy chirp records");
+    TDC_CK(cudaMemcpyAsync(p->skip.p, skip.data(), skip.size() * sizeof(SkipPoint), cudaMemcpyHostToDevice, st),
+           "copy skip table");
+    TDC_CK(cudaMemcpyAsync(p->gs.p, gs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "copy freq table");
+    TDC_CK(cudaMemcpyAsync(p->pos_base.p, base.data(), (size_t)C * 24, cudaMemcpyHostToDevice, st),
+           "copy base positions");
+    p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)n_rec * sizeof(ChirpRec) +
+                          (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
+    TDC_CK(cudaEventRecord(p->ev[1], st), "event");
+
+    TDC_CK(launch_range_window(p->wr.as<float>(), S, o.range_win, st), "range window kernel");
+    TDC_CK(launch_prewindow(p->xw.as<float2>(), p->wr.as<float>(), C, S, s_pad, st), "prewindow kernel");
+    launches += 2;
+    // The host vectors above are read by the async copies: wait before they go out of scope.
+    TDC_CK(cudaStreamSynchronize(st), "prepare sync");
+
+    p->opts = o;
+    p->prepared = true;
+    p->plan_path = -1;  // job parameters changed
+    return TDC_OK;
+}
+
+// Device grid from a host (FP32 or FP64) grid.
+int upload_grid(tdc_processor *p, int &launches)
+{
+    if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
+    const long long P = (long long)p->rows * p->cols;
+    p->P = P;
+    for (int k = 0; k < 3; ++k) {
+        p->grid_min[k] = std::numeric_limits<double>::infinity();
+        p->grid_max[k] = -std::numeric_limits<double>::infinity();
+    }
+    for (long long i = 0; i < P; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double v = p->grid64 ? p->grid64[3 * i + k] : (double)p->grid[3 * i + k];
+            p->grid_min[k] = std::min(p->grid_min[k], v);
+            p->grid_max[k] = std::max(p->grid_max[k], v);
+        }
+    cudaStream_t st = p->stream;
+    const size_t elt = p->grid64 ? 8 : 4;
+    TDC_CK(p->grid_stage.ensure((size_t)P * 3 * elt), "alloc grid staging");
+    TDC_CK(p->grid_hi.ensure((size_t)P * 16), "alloc grid");
+    TDC_CK(cudaMemcpyAsync(p->grid_stage.p, p->grid64 ? (const void *)p->grid64 : (const void *)p->grid,
+                           (size_t)P * 3 * elt, cudaMemcpyHostToDevice, st),
+           "copy grid");
+    p->stats.h2d_bytes += (int64_t)P * 3 * elt;
+    if (p->grid64) {
+        TDC_CK(p->grid_lo.ensure((size_t)P * 16), "alloc grid");
+        TDC_CK(launch_grid_from_f64(p->grid_stage.as<double>(), P, p->grid_hi.as<float4>(),
+                                    p->grid_lo.as<float4>(), st),
+               "grid kernel");
+        p->grid_lo_valid = true;
+    } else {
+        TDC_CK(launch_grid_from_f32(p->grid_stage.as<float>(), P, p->grid_hi.as<float4>(), st), "grid kernel");
+        p->grid_lo_valid = false;
+    }
+    launches += 1;
+    return TDC_OK;
+}
+
+int choose_path(const tdc_processor *p)
+{
+    if (!p->per_chirp) return TDC_PATH_GENERAL;
+    const double rmax = max_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
+    const double dev = 2.0 * M_PI * 2.0 * p->resid_hz * rmax / kC0;
+    if (dev > kUniformPhaseTolRad) return TDC_PATH_GENERAL;
+    if (p->precision == TDC_PRECISION_FP64_PHASE) return TDC_PATH_FP64_PHASE;
+    if (focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)p->s_pad * 8 + sizeof(ChirpRec), 128) >
+        227 * 1024)
+        return TDC_PATH_GENERAL;
+    return TDC_PATH_FP32_BULK;
+}
+
+// Split the chirps into groups so that tiles x groups units fill whole waves of `slots`.
+void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg)
+{
+    const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
+    double best = std::numeric_limits<double>::infinity();
+    n_groups = 1;
+    cpg = C;
+    const int gmax = std::max(1, std::min(C, 1024));
+    for (int g = 1; g <= gmax; ++g) {
+        const int c = (C + g - 1) / g;
+        const int geff = (C + c - 1) / c;
+        if (geff != g) continue;
+        const long long units = n_tiles * geff;
+        if (units > (1LL << 24)) break;
+        const long long waves = (units + slots - 1) / slots;
+        const double cost = (double)waves * (c + 0.5);
+        if (cost < best - 1e-9) {
+            best = cost;
+            n_groups = geff;
+            cpg = c;
+        }
+    }
+}
+
+// Scratch layout of one focus: [status words | job | units | partials].
+struct ScratchLayout {
+    size_t off_job, off_units, off_partial, total;
+};
+
+ScratchLayout scratch_layout(long long P, int n_units, int n_groups)
+{
+    ScratchLayout L;
+    L.off_job = 256;
+    L.off_units = round_up(L.off_job + sizeof(FocusJob), 256);
+    L.off_partial = round_up(L.off_units + (size_t)n_units * sizeof(FocusUnit), 256);
+    L.total = L.off_partial + (size_t)n_groups * (size_t)P * 16;
+    return L;
+}
+
+int stage_bytes_for(int s_pad, int &cb)
+{
+    const int row = s_pad * 8 + (int)sizeof(ChirpRec);
+    cb = std::max(1, 16640 / row);
+    return (int)round_up((size_t)cb * row, 128);
+}
+
+// Focus the resident acquisition onto the resident grid: image_dev (complex float [P]).
+int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &launches)
+{
+    if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
+    if (p->P <= 0) return fail(TDC_ERR_STATE, "no focus grid");
+    const int path = choose_path(p);
+    const long long P = p->P;
+    const int C = p->C;
+
+    int cb = 1;
+    const int stage_bytes = stage_bytes_for(p->s_pad, cb);
+    int slots;
+    if (path == TDC_PATH_FP32_BULK) {
+        const int bps = focus_fp32_blocks_per_sm(stage_bytes);
+        if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
+        slots = p->n_sm * bps;
+    } else {
+        slots = p->n_sm * 4;
+    }
+
+    if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots) {
+        plan_groups(P, C, slots, p->plan_groups, p->plan_cpg);
+        const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
+        p->units_host.clear();
+        p->units_host.reserve((size_t)(n_tiles * p->plan_groups));
+        for (long long t = 0; t < n_tiles; ++t)
+            for (int g = 0; g < p->plan_groups; ++g) p->units_host.push_back(FocusUnit{0, (int)t, g, 0});
+        p->plan_path = path;
+        p->plan_P = P;
+        p->plan_C = C;
+        p->plan_slots = slots;
+        p->plan_uploaded = false;
+    }
+    const int n_units = (int)p->units_host.size();
+    const ScratchLayout L = scratch_layout(P, n_units, p->plan_groups);
+    if (L.total > p->scratch.cap) {
+        TDC_CK(p->scratch.ensure(L.total), "alloc focus scratch");
+        p->plan_uploaded = false;
+    }
+    unsigned char *scr = p->scratch.as<unsigned char>();
+
+    FocusJob job;
+    std::memset(&job, 0, sizeof(job));
+    job.xw = p->xw.as<const float4>();
+    job.chirps = p->chirps.as<const ChirpRec>();
+    job.grid_hi = p->grid_hi.as<const float4>();
+    job.grid_lo = p->grid_lo_valid ? p->grid_lo.as<const float4>() : nullptr;
+    job.skip = p->skip.as<const SkipPoint>();
+    job.gs = p->gs.as<const double>();
+    job.partial = reinterpret_cast<float4 *>(scr + L.off_partial);
+    job.P = P;
+    job.C = C;
+    job.S = p->S;
+    job.s_pad = p->s_pad;
+    job.n_groups = p->plan_groups;
+    job.chirps_per_group = p->plan_cpg;
+    job.chunk = kChunk;
+    job.stage_chirps = cb;
+    job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
+    job.n_tiles = (int)((P + kFocusTile - 1) / kFocusTile);
+    job.per_sample = p->per_chirp ? 0 : 1;
+    const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
+    split_dd(g0, job.g0_hi, job.g0_lo);
+    split_dd(g1, job.g1, job.g1_lo);
+    job.two_over_lambda = 2.0f / p->lambda;
+    job.half_bw = p->opts.bw / 2.0f;
+    job.inv_bw = 1.0f / p->opts.bw;
+    job.az_a = kAzimuthA;
+
+    TDC_CK(cudaMemcpyAsync(scr + L.off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");
+    if (!p->plan_uploaded) {
+        TDC_CK(cudaMemcpyAsync(scr + L.off_units, p->units_host.data(), (size_t)n_units * sizeof(FocusUnit),
+                               cudaMemcpyHostToDevice, st),
+               "copy units");
+        p->plan_uploaded = true;
+    }
+    TDC_CK(cudaMemsetAsync(scr, 0, 8, st), "reset counter");
+    const FocusJob *jobs_dev = reinterpret_cast<const FocusJob *>(scr + L.off_job);
+    const FocusUnit *units_dev = reinterpret_cast<const FocusUnit *>(scr + L.off_units);
+    int *counter = reinterpret_cast<int *>(scr);
+    int *status = counter + 1;
+    if (path == TDC_PATH_FP32_BULK) {
+        const int grid = std::min(n_units, slots);
+        TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, st),
+               "focus kernel");
+    } else {
+        TDC_CK(launch_focus_fp64(jobs_dev, units_dev, n_units, status, p->per_chirp ? 0 : 1, st),
+               "focus kernel (fp64)");
+    }
+    TDC_CK(launch_focus_reduce(job.partial, p->plan_groups, P, image_dev, st), "reduce kernel");
+    launches += 2;
+    p->stats.path = path;
+    p->stats.correlations = (int64_t)P * C * p->S;
+    return TDC_OK;
+}
+
+int read_status(tdc_processor *p)
+{
+    int status = 0;
+    TDC_CK(cudaMemcpy(&status, p->scratch.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+    if (status & kStatusTimeout) return fail(TDC_ERR_TIMEOUT, "focus kernel wait timed out");
+    return TDC_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
+    return ms;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+const char *tdc_last_error(void) { return g_err.c_str(); }
+int tdc_abi_version(void) { return TDC_GB300_ABI_VERSION; }
+
+int tdc_processor_create(int gpu_num, tdc_processor **out)
+{
+    if (!out) return fail(TDC_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(gpu_num);
+    if (e != cudaSuccess)
+        return fail(TDC_ERR_CUDA, std::string("Failed to set cuda device: ") + cudaGetErrorString(e));
+    tdc_processor *p = new (std::nothrow) tdc_processor();
+    if (!p) return fail(TDC_ERR_NO_MEMORY, "out of host memory");
+    p->device = gpu_num;
+    e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, gpu_num);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&p->ev[i]);
+    if (e != cudaSuccess) {
+        tdc_processor_destroy(p);
+        return cuda_fail(e, "processor init");
+    }
+    *out = p;
+    return TDC_OK;
+}
+
+int tdc_processor_destroy(tdc_processor *p)
+{
+    if (!p) return TDC_OK;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (auto &ev : p->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return TDC_OK;
+}
+
+int tdc_processor_set_raw_data(tdc_processor *p, const float *raw_iq, const float *pri_times,
+                               const float *sample_times, const float *position, const float *velocity,
+                               const float *attitude, int n_pri, int n_samples, float mod_rate, float start_freq,
+                               const float *body_boresight)
+{
+    if (int rc = check_proc(p)) return rc;
+    // tdcprocessor.cpp:189-195
+    if (n_pri <= 0) return fail(TDC_ERR_INVALID_ARGUMENT, "nPri must be greater than 0");
+    if (n_samples <= 0) return fail(TDC_ERR_INVALID_ARGUMENT, "nSamples must be greater than 0");
+    if (!raw_iq || !sample_times || !position || !body_boresight)
+        return fail(TDC_ERR_INVALID_ARGUMENT, "null input array");
+    p->raw = raw_iq;
+    p->pri_times = pri_times;
+    p->sample_times = sample_times;
+    p->pos = position;
+    p->vel = velocity;
+    p->att = attitude;
+    p->C = n_pri;
+    p->S = n_samples;
+    p->mod_rate = mod_rate;
+    p->start_freq = start_freq;
+    for (int k = 0; k < 3; ++k) p->bore[k] = body_boresight[k];
+    // tdcprocessor.cpp:204-208: float subtraction, then double, then cast to float.
+    const float chirp_time_f = sample_times[n_samples - 1] - sample_times[0];
+    const double chirp_time = chirp_time_f;
+    const double end_freq = (double)start_freq + ((double)mod_rate * chirp_time);
+    const double centre = ((double)start_freq + end_freq) / 2.0;
+    p->lambda = (float)(kC0 / centre);
+    p->pos64 = nullptr;
+    p->has_raw = true;
+    p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_set_focus_grid(tdc_processor *p, const float *focus_grid, int n_rows, int n_cols)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (n_rows < 0 || n_cols < 0) return fail(TDC_ERR_INVALID_ARGUMENT, "negative grid shape");
+    if (!focus_grid && (long long)n_rows * n_cols > 0) return fail(TDC_ERR_INVALID_ARGUMENT, "null focus grid");
+    p->grid = focus_grid;
+    p->grid64 = nullptr;
+    p->rows = n_rows;
+    p->cols = n_cols;
+    p->has_grid = true;
+    return TDC_OK;
+}
+
+int tdc_processor_set_focus_grid_f64(tdc_processor *p, const double *focus_grid, int n_rows, int n_cols)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (n_rows < 0 || n_cols < 0) return fail(TDC_ERR_INVALID_ARGUMENT, "negative grid shape");
+    if (!focus_grid && (long long)n_rows * n_cols > 0) return fail(TDC_ERR_INVALID_ARGUMENT, "null focus grid");
+    p->grid = nullptr;
+    p->grid64 = focus_grid;
+    p->rows = n_rows;
+    p->cols = n_cols;
+    p->has_grid = true;
+    return TDC_OK;
+}
+
+int tdc_processor_set_chirp_positions_f64(tdc_processor *p, const double *position_f64, int n_pri)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called first");
+    if (position_f64 && n_pri != p->C) return fail(TDC_ERR_SHAPE, "position shape is incorrect");
+    p->pos64 = position_f64;
+    p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_set_precision(tdc_processor *p, int precision)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (precision != TDC_PRECISION_FP32_BULK && precision != TDC_PRECISION_FP64_PHASE)
+        return fail(TDC_ERR_INVALID_ARGUMENT, "unknown precision");
+    p->precision = precision;
+    return TDC_OK;
+}
+
+int tdc_processor_set_skip_test(tdc_processor *p, int enable)
+{
+    if (int rc = check_proc(p)) return rc;
+    p->skip_test = enable ? 1 : 0;
+    p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_start(tdc_processor *p, float doppler_win_center, float doppler_bandwidth, int dop_centroid_win,
+                        int apply_range_win, int doppler_win_taper)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called before start()");
+    if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
+    const auto t0 = std::chrono::steady_clock::now();
+    stats_reset(p);
+    int launches = 0;
+    StartOpts o;
+    o.center = doppler_win_center;
+    o.bw = doppler_bandwidth;
+    o.centroid = dop_centroid_win != 0;
+    o.range_win = apply_range_win != 0;
+    o.taper = doppler_win_taper != 0;
+    o.skip_test = p->skip_test;
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    cudaStream_t st = p->stream;
+    TDC_CK(cudaEventRecord(p->ev[0], st), "event");
+    if (int rc = prepare(p, o, launches)) return rc;
+    if (int rc = upload_grid(p, launches)) return rc;
+    TDC_CK(cudaEventRecord(p->ev[2], st), "event");
+    const long long P = p->P;
+    TDC_CK(p->image_dev.ensure((size_t)P * 8), "alloc image");
+    if (P > 0) {
+        if (int rc = focus_resident(p, p->image_dev.as<float2>(), st, launches)) return rc;
+    }
+    TDC_CK(cudaEventRecord(p->ev[3], st), "event");
+    TDC_CK(p->image_host.ensure((size_t)P * 8), "alloc host image");
+    if (P > 0) {
+        TDC_CK(cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st),
+               "copy image");
+    }
+    TDC_CK(cudaEventRecord(p->ev[4], st), "event");
+    // tdcprocessor.cpp:149-155: report any asynchronous failure of the launches.
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return fail(TDC_ERR_CUDA, std::string("Cuda runtime error occured during processing: ") +
+                                      cudaGetErrorString(e));
+    if (P > 0) {
+        if (int rc = read_status(p)) return rc;
+    }
+    p->image_valid = true;
+    p->stats.h2d_ms = elapsed(p->ev[0], p->ev[1]);
+    p->stats.prep_ms = elapsed(p->ev[1], p->ev[2]);
+    p->stats.focus_ms = elapsed(p->ev[2], p->ev[3]);
+    p->stats.d2h_ms = elapsed(p->ev[3], p->ev[4]);
+    p->stats.d2h_bytes = (int64_t)P * 8;
+    p->stats.kernel_launches = launches;
+    p->stats.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return TDC_OK;
+}
+
+const float *tdc_processor_image_buffer(const tdc_processor *p)
+{
+    if (!p || !p->image_valid) return nullptr;
+    return static_cast<const float *>(p->image_host.p);
+}
+
+int tdc_processor_grid_shape(const tdc_processor *p, int *n_rows, int *n_cols)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (n_rows) *n_rows = p->rows;
+    if (n_cols) *n_cols = p->cols;
+    return TDC_OK;
+}
+
+int tdc_processor_last_stats(const tdc_processor *p, tdc_start_stats *out)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!out) return fail(TDC_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = p->stats;
+    return TDC_OK;
+}
+
+// ---- device-resident entry points (for torch callers, benchmarks, autofocus) ----
+
+int tdc_processor_prepare(tdc_processor *p, float doppler_win_center, float doppler_bandwidth,
+                          int dop_centroid_win, int apply_range_win, int doppler_win_taper)
+{
+    if (int rc = check_proc(p)) return rc;
+    StartOpts o;
+    o.center = doppler_win_center;
+    o.bw = doppler_bandwidth;
+    o.centroid = dop_centroid_win != 0;
+    o.range_win = apply_range_win != 0;
+    o.taper = doppler_win_taper != 0;
+    o.skip_test = p->skip_test;
+    int launches = 0;
+    return prepare(p, o, launches);
+}
+
+int tdc_processor_upload_grid(tdc_processor *p)
+{
+    if (int rc = check_proc(p)) return rc;
+    int launches = 0;
+    if (int rc = upload_grid(p, launches)) return rc;
+    TDC_CK(cudaStreamSynchronize(p->stream), "grid sync");
+    return TDC_OK;
+}
+
+int tdc_processor_focus_device(tdc_processor *p, float *image_dev, void *stream)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!image_dev && p->P > 0) return fail(TDC_ERR_INVALID_ARGUMENT, "null image");
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    int launches = 0;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+    return focus_resident(p, reinterpret_cast<float2 *>(image_dev), st, launches);
+}
+
+int tdc_processor_check(tdc_processor *p, void *stream)
+{
+    if (int rc = check_proc(p)) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+    TDC_CK(cudaStreamSynchronize(st), "focus sync");
+    if (p->scratch.p) return read_status(p);
+    return TDC_OK;
+}
+
+int tdc_processor_num_pixels(const tdc_processor *p, int64_t *n)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (n) *n = p->P;
+    return TDC_OK;
+}
+
+int tdc_processor_path(const tdc_processor *p)
+{
+    if (!p || !p->prepared || p->P <= 0) return -1;
+    return choose_path(p);
+}
+
+int tdc_range_window(float *w_dev, int n_samples, int apply_range_win, void *stream)
+{
+    if (n_samples <= 0) return fail(TDC_ERR_INVALID_ARGUMENT, "nSamples must be greater than 0");
+    if (!w_dev) return fail(TDC_ERR_INVALID_ARGUMENT, "null window");
+    TDC_CK(launch_range_window(w_dev, n_samples, apply_range_win, static_cast<cudaStream_t>(stream)),
+           "range window kernel");
+    return TDC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,353 @@
+// tdc_focus.cu -- FP32-bulk fused focus kernel of the GB300 TDC engine.
+//
+// Replaces the reference's per-(chunk, pixel) sequence createWindowKernel ->
+// referenceResponseKernel -> correlateWithReference -> nppsSum_32fc -> addToImage
+// (tdc-lib/src/tdckernels.cu:70-315, driven from tdcprocessor.cpp:77-156) with one
+// persistent launch over work units (pixel tile x chirp group):
+//
+//   I(T) = sum_c w_az(T, c) * sum_s xw[c, s] * exp(+j 2 pi (2 R_c(T) f_s / c0)),
+//   xw = range-windowed raw samples, f_s = f_0 + s df (uniform sample spacing).
+//
+// Per (pixel, chirp): R in double-float, phase at sample 0 (alpha) reduced
+// modulo one cycle in double-float, per-sample step beta. Per sample the
+// phasor is exp(j 2 pi (alpha + (bL + k) beta)) = e^{j2pi alpha} QL^b p_k, with
+// p_k = e^{j 2 pi k beta} (k < L) kept in registers and QL = e^{j 2 pi L beta}.
+// The chirp sum is evaluated by Horner's rule over the blocks b (last block
+// first): H <- H * QL + sum_k x_{bL+k} p_k, so every sample costs exactly one
+// complex multiply-add (4 FFMA) and no separate phasor advance. Block phasors
+// never accumulate more than S/L rotations of an accurately computed QL.
+// Chirp sums are accumulated per pixel with Kahan compensation; partial sums
+// per chirp group are combined in FP64 by focus_reduce_kernel in a fixed order,
+// so results do not depend on scheduling.
+//
+// Chirp sample rows and trajectory records are staged global->shared with
+// cp.async.bulk on an mbarrier pipeline (kFocusStages deep) and read back as
+// broadcast 128-bit shared loads shared by all 512 pixels of the tile.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tdc_device.cuh"
+#include "tdc_internal.h"
+
+namespace tdc {
+
+namespace {
+
+constexpr int kL = 8;  // in-block phasor table length
+
+struct SharedPixel {
+    float t[kFocusPT * 6][kFocusThreads];  // (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo) per pixel slot
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// One Horner block for one pixel: H <- H * ql + sum_{k<L} x_k p_k (p_0 = 1).
+__device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2 (&p)[kL - 1],
+                                               const float4 (&xv)[kL / 2])
+{
+    float tr = fmaf(h.x, ql.x, xv[0].x);
+    tr = fmaf(-h.y, ql.y, tr);
+    float ti = fmaf(h.x, ql.y, xv[0].y);
+    ti = fmaf(h.y, ql.x, ti);
+#pragma unroll
+    for (int k = 1; k < kL; ++k) {
+        const float xr = (k & 1) ? xv[k >> 1].z : xv[k >> 1].x;
+        const float xi = (k & 1) ? xv[k >> 1].w : xv[k >> 1].y;
+        tr = fmaf(xr, p[k - 1].x, tr);
+        tr = fmaf(-xi, p[k - 1].y, tr);
+        ti = fmaf(xr, p[k - 1].y, ti);
+        ti = fmaf(xi, p[k - 1].x, ti);
+    }
+    return make_float2(tr, ti);
+}
+
+__global__ void __launch_bounds__(kFocusThreads, 3)
+    focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
+                      int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full_bar[kFocusStages];
+    __shared__ int s_unit;
+    __shared__ FocusJob sJ;
+
+    SharedPixel &sp = *reinterpret_cast<SharedPixel *>(smem + kFocusStages * stage_bytes);
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        for (int i = 0; i < kFocusStages; ++i) mbar_init(&full_bar[i], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    uint32_t n_issued = 0;    // producer (thread 0) only
+    uint32_t n_consumed = 0;  // uniform across the CTA
+
+    for (;;) {
+        if (tid == 0) {
+            s_unit = atomicAdd(counter, 1);
+        }
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= n_units) break;
+        const FocusUnit un = units[u];
+        if (tid < (int)(sizeof(FocusJob) / sizeof(int))) {
+            reinterpret_cast<int *>(&sJ)[tid] = reinterpret_cast<const int *>(&jobs[un.job])[tid];
+        }
+        __syncthreads();
+
+        const int C = sJ.C;
+        const int c0 = un.group * sJ.chirps_per_group;
+        const int c1 = min(C, c0 + sJ.chirps_per_group);
+        const int CB = sJ.stage_chirps;
+        const int nblk = (c1 - c0 + CB - 1) / CB;
+        const int s_pad = sJ.s_pad;
+        const uint32_t row_bytes = static_cast<uint32_t>(s_pad) * 8u;
+        const float4 *__restrict__ xw = sJ.xw;
+        const ChirpRec *__restrict__ chirps = sJ.chirps;
+
+        // Producer: issue the first stages of this unit.
+        if (tid == 0) {
+            const int npro = nblk < kFocusStages ? nblk : kFocusStages;
+            for (int j = 0; j < npro; ++j) {
+                const int cb0 = c0 + j * CB;
+                const int cnt = min(CB, c1 - cb0);
+                const int st = n_issued % kFocusStages;
+                unsigned char *base = smem + st * stage_bytes;
+                const uint32_t bx = cnt * row_bytes, br = cnt * (uint32_t)sizeof(ChirpRec);
+                mbar_arrive_expect_tx(&full_bar[st], bx + br);
+                bulk_g2s(base, xw + (size_t)cb0 * (s_pad / 2), bx, &full_bar[st]);
+                bulk_g2s(base + CB * row_bytes, chirps + cb0, br, &full_bar[st]);
+                ++n_issued;
+            }
+        }
+
+        // Pixel coordinates of this thread's PT slots -> shared (own column).
+        const long long tile_base = (long long)un.tile * kFocusTile;
+        const long long P = sJ.P;
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            const long long p = tile_base + i * kFocusThreads + tid;
+            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+            if (p < P) {
+                hi = __ldg(&sJ.grid_hi[p]);
+                if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[p]);
+            }
+            sp.t[i * 6 + 0][tid] = hi.x;
+            sp.t[i * 6 + 1][tid] = hi.y;
+            sp.t[i * 6 + 2][tid] = hi.z;
+            sp.t[i * 6 + 3][tid] = lo.x;
+            sp.t[i * 6 + 4][tid] = lo.y;
+            sp.t[i * 6 + 5][tid] = lo.z;
+        }
+
+        const float g0h = sJ.g0_hi, g0l = sJ.g0_lo, g1 = sJ.g1;
+        const float g1l = sJ.g1_lo;
+        const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
+        const bool taper = (sJ.flags & kFlagTaper) != 0;
+        const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
+        const int chunk = sJ.chunk;
+        const SkipPoint *__restrict__ skip = sJ.skip;
+        const int nb = s_pad / kL;
+
+        float2 sum[kFocusPT], comp[kFocusPT];
+        float wskip[kFocusPT];
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            sum[i] = make_float2(0.f, 0.f);
+            comp[i] = make_float2(0.f, 0.f);
+            wskip[i] = 1.0f;
+        }
+        int cur_chunk = -1;
+        bool timed_out = false;
+
+        for (int j = 0; j < nblk; ++j) {
+            const int st = n_consumed % kFocusStages;
+            const uint32_t parity = (n_consumed / kFocusStages) & 1u;
+            const bool ok = mbar_wait_bounded(&full_bar[st], parity, kWaitLimitNs);
+            if (__syncthreads_or(!ok)) {
+                timed_out = true;
+                break;
+            }
+            const unsigned char *base = smem + st * stage_bytes;
+            const float4 *xs_stage = reinterpret_cast<const float4 *>(base);
+            const ChirpRec *recs = reinterpret_cast<const ChirpRec *>(base + CB * row_bytes);
+            const int cb0 = c0 + j * CB;
+            const int cnt = min(CB, c1 - cb0);
+
+            for (int cc = 0; cc < cnt; ++cc) {
+                const int c = cb0 + cc;
+                if (skip_test) {
+                    const int k = c / chunk;
+                    if (k != cur_chunk) {
+                        cur_chunk = k;
+#pragma unroll
+                        for (int i = 0; i < kFocusPT; ++i) {
+                            wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, sp.t[i * 6 + 0][tid],
+                                                        sp.t[i * 6 + 1][tid], sp.t[i * 6 + 2][tid], tol,
+                                                        half_bw)
+                                           ? 1.0f
+                                           : 0.0f;
+                        }
+                    }
+                }
+                const ChirpRec r = recs[cc];
+                const float4 *xs = xs_stage + (size_t)cc * (s_pad / 2);
+
+                float2 p[kFocusPT][kL - 1];
+                float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
+#pragma unroll
+                for (int i = 0; i < kFocusPT; ++i) {
+                    float dxh, dxl, dyh, dyl, dzh, dzl;
+                    dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
+                    dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
+                    dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
+                    float rh, rl, rs, dh;
+                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
+                    const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
+                    // beta = (g1 + g1l) * (rh + rl) cycles per sample, reduced modulo 1.
+                    float bh = g1 * rh;
+                    float bl = fmaf(g1, rh, -bh);
+                    bl = fmaf(g1, rl, bl);
+                    bl = fmaf(g1l, rh, bl);
+                    bh -= rintf(bh);
+                    float s1, c1s;
+                    __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
+                    p[i][0] = make_float2(c1s, s1);
+#pragma unroll
+                    for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
+                    const float lbh = (float)kL * bh;  // exact
+                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
+                    float sl, cl;
+                    sincospif(2.0f * lfr, &sl, &cl);
+                    ql[i] = make_float2(cl, sl);
+                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                    const float w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                    float sa, ca;
+                    __sincosf(kTwoPiF * alpha, &sa, &ca);
+                    q0[i] = make_float2(w * ca, w * sa);
+                    h[i] = make_float2(0.f, 0.f);
+                }
+
+                // Horner over blocks, last block first.
+#pragma unroll 2
+                for (int b = nb - 1; b >= 0; --b) {
+                    float4 xv[kL / 2];
+#pragma unroll
+                    for (int m = 0; m < kL / 2; ++m) xv[m] = xs[b * (kL / 2) + m];
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) h[i] = horner_block(h[i], ql[i], p[i], xv);
+                }
+
+#pragma unroll
+                for (int i = 0; i < kFocusPT; ++i) {
+                    const float2 v = cmul(q0[i], h[i]);
+                    // Kahan: comp carries the rounding error of the running sum (true = sum - comp).
+                    const float yr = v.x - comp[i].x, yi = v.y - comp[i].y;
+                    const float tr = sum[i].x + yr, ti = sum[i].y + yi;
+                    comp[i].x = (tr - sum[i].x) - yr;
+                    comp[i].y = (ti - sum[i].y) - yi;
+                    sum[i].x = tr;
+                    sum[i].y = ti;
+                }
+            }
+
+            __syncthreads();  // every thread is done with this stage
+            ++n_consumed;
+            if (tid == 0 && j + kFocusStages < nblk) {
+                const int jn = j + kFocusStages;
+                const int cb0n = c0 + jn * CB;
+                const int cntn = min(CB, c1 - cb0n);
+                const int stn = n_issued % kFocusStages;
+                unsigned char *basen = smem + stn * stage_bytes;
+                const uint32_t bx = cntn * row_bytes, br = cntn * (uint32_t)sizeof(ChirpRec);
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&full_bar[stn], bx + br);
+                bulk_g2s(basen, xw + (size_t)cb0n * (s_pad / 2), bx, &full_bar[stn]);
+                bulk_g2s(basen + CB * row_bytes, chirps + cb0n, br, &full_bar[stn]);
+                ++n_issued;
+            }
+        }
+
+        if (timed_out) {
+            // Let the copies still in flight land before the CTA exits, then report.
+            if (tid == 0) {
+                for (uint32_t k = n_consumed; k < n_issued; ++k) {
+                    mbar_wait_bounded(&full_bar[k % kFocusStages], (k / kFocusStages) & 1u, kWaitLimitNs);
+                }
+                atomicOr(status, kStatusTimeout);
+            }
+            __syncthreads();
+            return;
+        }
+
+        float4 *__restrict__ part = sJ.partial + (size_t)un.group * P;
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            const long long pidx = tile_base + i * kFocusThreads + tid;
+            if (pidx < P) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
+        }
+        __syncthreads();  // sJ / sp are rewritten by the next unit
+    }
+}
+
+// image[p] = sum over groups of (sum - comp), added in FP64 in group order.
+__global__ void focus_reduce_kernel(const float4 *__restrict__ partial, int n_groups, long long P,
+                                    float2 *__restrict__ image)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    double re = 0.0, im = 0.0;
+    for (int g = 0; g < n_groups; ++g) {
+        const float4 v = partial[(size_t)g * P + p];
+        re += (double)v.x - (double)v.z;
+        im += (double)v.y - (double)v.w;
+    }
+    image[p] = make_float2((float)re, (float)im);
+}
+
+}  // namespace
+
+int focus_fp32_smem_bytes(int stage_bytes)
+{
+    return kFocusStages * stage_bytes + (int)sizeof(SharedPixel);
+}
+
+int focus_fp32_blocks_per_sm(int stage_bytes)
+{
+    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    if (cudaFuncSetAttribute(focus_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess) {
+        return 0;
+    }
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel, kFocusThreads, smem) !=
+        cudaSuccess) {
+        return 0;
+    }
+    return blocks;
+}
+
+cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
+                              int *status_dev, int stage_bytes, int grid_ctas, cudaStream_t st)
+{
+    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    cudaError_t e = cudaFuncSetAttribute(focus_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    focus_fp32_kernel<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
+                                                               status_dev, stage_bytes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image, cudaStream_t st)
+{
+    if (P <= 0) return cudaSuccess;
+    const int threads = 256;
+    const long long blocks = (P + threads - 1) / threads;
+    focus_reduce_kernel<<<(unsigned)blocks, threads, 0, st>>>(partial, n_groups, P, image);
+    return cudaGetLastError();
+}
+
+}  // namespace tdc

@@ -1,0 +1,108 @@
+// tdc_internal.h -- structures shared by the host code and the kernels of the
+// GB300 TDC engine. Not part of the public ABI (include/tdc_gb300.h is).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace tdc {
+
+constexpr double kC0 = 299792458.0;  // SPEED_OF_LIGHT, tdcprocessor.cpp:37
+constexpr int kChunk = 128;          // PRI_CHUNKSIZE, tuning.h:18
+constexpr float kRangeA = 25.0f / 46.0f;    // RANGE_WINDOW_A_PARAMETER, tuning.h:31
+constexpr float kAzimuthA = 25.0f / 46.0f;  // AZIMUTH_WINDOW_A_PARAMETER, tuning.h:38
+
+// Focus tile geometry of the FP32-bulk kernel: 128 threads x 4 pixels.
+constexpr int kFocusThreads = 128;
+constexpr int kFocusPT = 4;
+constexpr int kFocusTile = kFocusThreads * kFocusPT;
+constexpr int kFocusStages = 3;
+constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows stay 128-byte sized)
+
+// One chirp's trajectory record, 48 bytes (3 x float4):
+//   p_hi.xyz  antenna position, high float of a double-float pair; p_hi.w = Doppler window centre [Hz]
+//   p_lo.xyz  low float of the position pair; p_lo.w = 0
+//   vel.xyz   velocity; vel.w = 0
+struct __align__(16) ChirpRec {
+    float4 p_hi;
+    float4 p_lo;
+    float4 vel;
+};
+static_assert(sizeof(ChirpRec) == 48, "ChirpRec must be 48 bytes");
+
+// One sample point of the reference's chunk skip test (tdcprocessor.cpp:355-378).
+struct __align__(16) SkipPoint {
+    float4 pos_fdc;  // position xyz, window centre
+    float4 vel;      // velocity xyz, 0
+};
+static_assert(sizeof(SkipPoint) == 32, "SkipPoint must be 32 bytes");
+
+enum FocusFlags : int {
+    kFlagTaper = 1,     // dopplerWinTaper
+    kFlagSkipTest = 2,  // apply the per-chunk skip test
+};
+
+// Everything a focus kernel needs about one job (acquisition x grid).
+struct FocusJob {
+    const float4 *xw;        // [C][s_pad/2]: pairs of windowed complex samples
+    const ChirpRec *chirps;  // [C] (or [C][S] for per-sample trajectories)
+    const float4 *grid_hi;   // [P]
+    const float4 *grid_lo;   // [P] or nullptr
+    const SkipPoint *skip;   // [n_chunks][9]
+    const double *gs;        // [S] 2 f_s / c0 (FP64 kernels only)
+    float4 *partial;         // [n_groups][P]: (sum.re, sum.im, comp.re, comp.im)
+    long long P;
+    int C;
+    int S;
+    int s_pad;
+    int n_groups;
+    int chirps_per_group;
+    int chunk;
+    int stage_chirps;        // chirps per pipeline stage
+    int flags;
+    int n_tiles;
+    int per_sample;          // ChirpRec per sample instead of per chirp
+    float g0_hi, g0_lo;      // 2 f_0 / c0 as a double-float pair [cycles / m]
+    float g1;                // 2 df / c0 per sample [cycles / m]
+    float two_over_lambda;   // 2 / lambda_centre
+    float half_bw;           // dopplerBandwidth / 2
+    float inv_bw;            // 1 / dopplerBandwidth
+    float az_a;              // azimuth window a
+    float g1_lo;             // low part of g1 (double-float pair)
+};
+
+struct FocusUnit {
+    int job;
+    int tile;
+    int group;
+    int pad_;
+};
+
+// Kernel-side status bits (written to the status word in scratch).
+enum StatusBits : int {
+    kStatusTimeout = 1,
+};
+
+// ---- launchers (defined in the .cu files) ----
+cudaError_t launch_range_window(float *w, int n, int apply, cudaStream_t st);
+cudaError_t launch_prewindow(float2 *xw, const float *w, int C, int S, int s_pad, cudaStream_t st);
+cudaError_t launch_chirp_positions(ChirpRec *recs, const double *base, const double *off, int C, cudaStream_t st);
+cudaError_t launch_grid_from_f32(const float *grid, long long P, float4 *hi, cudaStream_t st);
+cudaError_t launch_grid_from_f64(const double *grid, long long P, float4 *hi, float4 *lo, cudaStream_t st);
+
+// FP32-bulk focus over a unit list. `jobs` and `units` are device arrays.
+cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
+                              int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,
+                              cudaStream_t st);
+// Plain FP64-phase focus (comparator and general fallback), one CTA per unit.
+cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
+                              int *status_dev, int per_sample, cudaStream_t st);
+cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image,
+                                cudaStream_t st);
+
+// Occupancy of the FP32-bulk kernel at a given dynamic shared memory size.
+int focus_fp32_blocks_per_sm(int stage_bytes);
+int focus_fp32_smem_bytes(int stage_bytes);
+
+}  // namespace tdc

@@ -1,0 +1,121 @@
+// tdc_prep.cu -- per-acquisition preparation kernels of the GB300 TDC engine:
+// the range window (tdc-lib/src/tdckernels.cu:32-64), its application to the
+// raw chirps once per start() instead of once per pixel, focus-grid layout
+// conversion and per-chirp position offsets (autofocus).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tdc_device.cuh"
+#include "tdc_internal.h"
+
+namespace tdc {
+
+namespace {
+
+// w[n] = a - (1 - a) cos(2 pi n / N) (periodic), a = 25/46, or all ones.
+__global__ void range_window_kernel(float *__restrict__ w, int n, int apply)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    w[i] = apply ? kRangeA - (1.0f - kRangeA) * cospif(2.0f * (float)i / (float)n) : 1.0f;
+}
+
+// In place on rows of s_pad complex samples (first S valid): x *= w[s]; padding -> 0.
+__global__ void prewindow_kernel(float2 *__restrict__ xw, const float *__restrict__ w, int C, int S, int s_pad)
+{
+    const long long total = (long long)C * s_pad;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int s = (int)(idx % s_pad);
+        float2 v = make_float2(0.f, 0.f);
+        if (s < S) {
+            const float ws = w[s];
+            const float2 x = xw[idx];
+            v = make_float2(x.x * ws, x.y * ws);
+        }
+        xw[idx] = v;
+    }
+}
+
+__global__ void grid_f32_kernel(const float *__restrict__ g, long long P, float4 *__restrict__ hi)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    hi[p] = make_float4(g[3 * p], g[3 * p + 1], g[3 * p + 2], 0.f);
+}
+
+__device__ __forceinline__ void split_dd(double v, float &h, float &l)
+{
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+__global__ void grid_f64_kernel(const double *__restrict__ g, long long P, float4 *__restrict__ hi,
+                                float4 *__restrict__ lo)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    float h[3], l[3];
+    for (int k = 0; k < 3; ++k) split_dd(g[3 * p + k], h[k], l[k]);
+    hi[p] = make_float4(h[0], h[1], h[2], 0.f);
+    lo[p] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
+// recs[c].p = base[c] + off[c] as double-float pairs (off may be null).
+__global__ void chirp_positions_kernel(ChirpRec *__restrict__ recs, const double *__restrict__ base,
+                                       const double *__restrict__ off, int C)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    float h[3], l[3];
+    for (int k = 0; k < 3; ++k) {
+        const double v = base[3 * c + k] + (off ? off[3 * c + k] : 0.0);
+        split_dd(v, h[k], l[k]);
+    }
+    ChirpRec r = recs[c];
+    r.p_hi = make_float4(h[0], h[1], h[2], r.p_hi.w);
+    r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
+    recs[c] = r;
+}
+
+}  // namespace
+
+cudaError_t launch_range_window(float *w, int n, int apply, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    range_window_kernel<<<(n + 127) / 128, 128, 0, st>>>(w, n, apply);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prewindow(float2 *xw, const float *w, int C, int S, int s_pad, cudaStream_t st)
+{
+    const long long total = (long long)C * s_pad;
+    if (total <= 0) return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    prewindow_kernel<<<(unsigned)blocks, 256, 0, st>>>(xw, w, C, S, s_pad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_from_f32(const float *grid, long long P, float4 *hi, cudaStream_t st)
+{
+    if (P <= 0) return cudaSuccess;
+    grid_f32_kernel<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(grid, P, hi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_from_f64(const double *grid, long long P, float4 *hi, float4 *lo, cudaStream_t st)
+{
+    if (P <= 0) return cudaSuccess;
+    grid_f64_kernel<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(grid, P, hi, lo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chirp_positions(ChirpRec *recs, const double *base, const double *off, int C, cudaStream_t st)
+{
+    if (C <= 0) return cudaSuccess;
+    chirp_positions_kernel<<<(C + 127) / 128, 128, 0, st>>>(recs, base, off, C);
+    return cudaGetLastError();
+}
+
+}  // namespace tdc

@@ -1,0 +1,145 @@
+"""CPU tests of the C-ABI boundary and the host-side mirror of the reference's
+Python interface (no compute: no GPU here)."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+def _declared_c_functions():
+    names = set()
+    for h in HEADERS:
+        text = h.read_text()
+        if 'extern "C"' not in text and "tdc_" not in text:
+            continue
+        body = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        body = re.sub(r"//[^\n]*", "", body)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(tdc_\w+)\s*\(", body, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_builds_and_exports_every_declared_symbol(engine_lib):
+    declared = _declared_c_functions()
+    assert "tdc_processor_start" in declared and "tdc_processor_focus_device" in declared
+    for name in sorted(declared):
+        assert hasattr(engine_lib, name), f"{name} declared in include/ but not exported"
+    out = subprocess.run(["nm", "-D", "--defined-only", engine_lib._name], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (tdc_\w+)", out))
+    assert declared <= exported
+    assert engine_lib.tdc_abi_version() == 1
+
+
+def test_binding_signatures_cover_the_header():
+    import _tdc_capi
+
+    bound = {name for name, _, _ in _tdc_capi.SIGNATURES}
+    assert _declared_c_functions() <= bound
+
+
+def test_library_is_sm103a_only(engine_lib):
+    log = (ROOT / "sarlab-tdc_gb300" / "_build" / "ptxas.log").read_text()
+    assert "sm_103a" in log
+    assert "spill stores" in log
+    # no kernel spills registers
+    assert not re.search(r"[1-9]\d* bytes spill stores", log)
+
+
+def test_error_mapping(engine_lib):
+    import _tdc_capi as L
+
+    L.check(0)
+    with pytest.raises(ValueError):
+        L.check(L.TDC_ERR_INVALID_ARGUMENT)
+    with pytest.raises(RuntimeError):
+        L.check(L.TDC_ERR_CUDA)
+    with pytest.raises(RuntimeError):
+        L.check(L.TDC_ERR_TIMEOUT)
+    with pytest.raises(MemoryError):
+        L.check(L.TDC_ERR_NO_MEMORY)
+
+
+def test_null_processor_is_rejected(engine_lib):
+    import _tdc_capi as L
+
+    rc = engine_lib.tdc_processor_start(None, 0.0, 1.0, 0, 0, 1)
+    assert rc == L.TDC_ERR_INVALID_ARGUMENT
+    assert "null processor" in L.last_error()
+    assert engine_lib.tdc_processor_image_buffer(None) is None
+
+
+def _unbound_processor():
+    import _sarlabtdc
+
+    p = object.__new__(_sarlabtdc.TdcProcessor)
+    p._h = None
+    return p
+
+
+def _args(C=4, S=8):
+    return dict(rawData=np.zeros((C, S), np.complex64), priTimes=np.zeros(C, np.float32),
+                sampleTimes=np.zeros(S, np.float32), position=np.zeros((C, S, 3), np.float32),
+                velocity=np.zeros((C, S, 3), np.float32), attitude=np.zeros((C, S, 4), np.float32),
+                modRate=1.0, startFreq=1.0, bodyBoresight=np.zeros(3, np.float32))
+
+
+@pytest.mark.parametrize("key,bad,msg", [
+    ("rawData", np.zeros(8, np.complex64), "rawData must be 2D"),
+    ("priTimes", np.zeros((4, 1), np.float32), "priTimes must be 1D"),
+    ("sampleTimes", np.zeros((8, 1), np.float32), "sampleTimes must be 1D"),
+    ("position", np.zeros((4, 8), np.float32), "position must be 3D"),
+    ("velocity", np.zeros((4, 8), np.float32), "velocity must be 3D"),
+    ("attitude", np.zeros((4, 8), np.float32), "attitude must be 3D"),
+    ("bodyBoresight", np.zeros((3, 1), np.float32), "bodyBoresight must be 1D"),
+    ("priTimes", np.zeros(5, np.float32), "priTimes shape is incorrect"),
+    ("sampleTimes", np.zeros(7, np.float32), "sampleTimes shape is incorrect"),
+    ("position", np.zeros((4, 8, 4), np.float32), "position shape is incorrect"),
+    ("velocity", np.zeros((4, 7, 3), np.float32), "velocity shape is incorrect"),
+    ("attitude", np.zeros((4, 8, 3), np.float32), "attitude shape is incorrect"),
+    ("bodyBoresight", np.zeros(4, np.float32), "bodyBoresight shape is incorrect"),
+])
+def test_setrawdata_shape_checks_mirror_the_reference(key, bad, msg):
+    """tdcprocessor_wrapper.cpp:54-113: the same checks, order and messages."""
+    p = _unbound_processor()
+    a = _args()
+    a[key] = bad
+    with pytest.raises(RuntimeError, match=msg):
+        p.setRawData(*a.values())
+
+
+def test_setfocusgrid_shape_checks():
+    p = _unbound_processor()
+    with pytest.raises(RuntimeError, match="focusGrid must be 3D"):
+        p.setFocusGrid(np.zeros((4, 3), np.float32))
+    with pytest.raises(RuntimeError, match="focusGrid shape is incorrect"):
+        p.setFocusGrid(np.zeros((4, 4, 2), np.float32))
+
+
+def test_setrawdata_positional_only_like_pybind():
+    import _sarlabtdc
+
+    p = _unbound_processor()
+    with pytest.raises(TypeError):
+        p.setRawData(**_args())
+    assert _sarlabtdc.TdcProcessor.start.__defaults__ == (True,)
+
+
+def test_product_never_touches_the_oracle():
+    pkg = ROOT / "sarlab-tdc_gb300"
+    for f in list(pkg.rglob("*.py")) + list(pkg.rglob("*.cu")) + list(pkg.rglob("*.cpp")) + \
+            list(pkg.rglob("*.h")) + list(pkg.rglob("*.cuh")):
+        text = f.read_text()
+        assert not re.search(r"(import\s+oracle|from\s+oracle|libtdc_oracle|libtdc_refmath|oracle/)", text), \
+            f"{f} imports or loads the oracle"
+
+
+def test_no_closed_copy_calls_in_sources():
+    # one cudaMemcpyAsync per copy; batch-copy entry points are not used anywhere
+    pkg = ROOT / "sarlab-tdc_gb300" / "csrc"
+    for f in pkg.iterdir():
+        assert "BatchAsync" not in f.read_text()

@@ -1,0 +1,247 @@
+"""GPU parity tests: the engine (through the C ABI, via the reference-shaped
+_sarlabtdc binding) against the FP64 oracle on the same inputs.
+
+Tolerances: the engine's stated accuracy against the FP64 oracle is
+relative L2 <= 1e-4 and max phase error <= 1e-3 rad over pixels within 40 dB of
+the peak. Tests whose Doppler windows have chirps close to the inclusive band
+edge (where FP32 and FP64 may take different sides) use only the L2 bound.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from sarlabtdc import scenes
+from tdc_testutil import max_phase_err, peak_err, problem_from_api, rel_l2, run_engine
+
+pytestmark = pytest.mark.gpu
+
+L2_TOL = 1e-4
+PHASE_TOL = 1e-3
+INF = float("inf")
+
+
+def _oracle(api, grid, start_args, pos64=None, grid64=False, pixels=None, skip_test=True):
+    c, b, cw, rw = start_args[:4]
+    taper = start_args[4] if len(start_args) > 4 else True
+    prob = problem_from_api(api, grid, pos64=pos64, grid64=grid64)
+    o = oracle.Opts(dopplerWinCenter=c, dopplerBandwidth=b, dopCentroidWin=cw, applyRangeWin=rw,
+                    dopplerWinTaper=taper, skip_test=skip_test)
+    return oracle.focus(prob, o, pixels=pixels)
+
+
+def _check(img, ref, l2=L2_TOL, phase=PHASE_TOL):
+    e_l2 = rel_l2(img, ref)
+    assert e_l2 <= l2, f"relative L2 {e_l2:.3e} > {l2:.1e}"
+    if phase is not None:
+        e_ph = max_phase_err(img, ref)
+        assert e_ph <= phase, f"max phase error {e_ph:.3e} rad > {phase:.1e}"
+    return e_l2
+
+
+def test_smoke_all_zero_inputs_like_reference_test(cuda_device):
+    """tdctest/tdctest.cpp:21-59: 20 x 20 grid, nPri = 750, nSamples = 1500, zeros everywhere,
+    B = 5 Hz, centroid windowing, range window. Antenna on every pixel -> NaN Doppler -> zero window."""
+    C, S = 750, 1500
+    api = dict(rawData=np.zeros((C, S), np.complex64), priTimes=np.zeros(C, np.float32),
+               sampleTimes=np.zeros(S, np.float32), position=np.zeros((C, S, 3), np.float32),
+               velocity=np.zeros((C, S, 3), np.float32), attitude=np.zeros((C, S, 4), np.float32),
+               modRate=1.0, startFreq=1.0, bodyBoresight=np.array([0, 1, 0], np.float32))
+    grid = np.zeros((20, 20, 3), np.float32)
+    img, stats, _ = run_engine(api, grid, (0.0, 5.0, True, True))
+    assert img.shape == (20, 20) and img.dtype == np.complex64
+    assert np.all(img == 0)
+    assert stats["kernel_launches"] >= 4
+
+
+def _scene_api(sc):
+    a = sc.api_arrays()
+    return a
+
+
+@pytest.mark.parametrize("n_samples", [128, 1, 17, 33, 1500])
+def test_parity_plain(cuda_device, n_samples):
+    sc = scenes.small_scene(seed=n_samples, n_pri=160, n_samples=n_samples, nx=19, ny=13, device="cuda")
+    api = _scene_api(sc)
+    args = (0.0, INF, False, False, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "fp32_bulk"
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref)
+
+
+def test_parity_range_window_and_partial_tiles(cuda_device):
+    sc = scenes.small_scene(seed=5, n_pri=300, n_samples=96, nx=33, ny=31, device="cuda")  # 1023 px
+    api = _scene_api(sc)
+    args = (0.0, INF, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref)
+    # single pixel
+    one = sc.grid[:1, :1]
+    img1, _, _ = run_engine(api, one, args)
+    _check(img1, ref[:1, :1], phase=None)
+    np.testing.assert_allclose(img1[0, 0], img[0, 0], rtol=2e-6)
+
+
+def _moving_api(sc, speed=0.05, yaw_sigma=0.02, seed=0):
+    """Per-chirp-constant velocity along the rail and a per-chirp attitude (yaw) jitter."""
+    rng = np.random.default_rng(seed)
+    api = sc.api_arrays()
+    C, S = sc.n_pri, sc.n_samples
+    vel = np.zeros((C, S, 3), np.float32)
+    vel[..., 0] = speed
+    ang = rng.normal(0, yaw_sigma, C)
+    att = np.zeros((C, S, 4), np.float32)
+    att[..., 0] = np.cos(ang / 2)[:, None]
+    att[..., 3] = np.sin(ang / 2)[:, None]
+    api["velocity"] = vel
+    api["attitude"] = att
+    return api
+
+
+@pytest.mark.parametrize("taper,centroid", [(True, True), (False, False), (True, False)])
+def test_parity_doppler_window_and_skip_test(cuda_device, taper, centroid):
+    """Finite Doppler band: per-chirp windows, tapered or rectangular, fixed centre or centroid,
+    and the per-chunk skip test (nPri = 750: a partial last chunk with stale staging rows)."""
+    sc = scenes.small_scene(seed=11, n_pri=750, n_samples=64, nx=21, ny=17, rail_len=0.75, device="cuda")
+    api = _moving_api(sc)
+    args = (2.0, 18.0, centroid, True, taper)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    # some pixels must actually be windowed / skipped for this to test anything
+    full = _oracle(api, sc.grid, (0.0, INF, False, True, taper)).reshape(img.shape)
+    assert rel_l2(ref, full) > 0.05
+    _check(img, ref, l2=2e-4, phase=None)
+
+
+def test_skip_test_can_be_disabled(cuda_device):
+    sc = scenes.small_scene(seed=12, n_pri=384, n_samples=32, nx=16, ny=16, rail_len=0.5, device="cuda")
+    api = _moving_api(sc, speed=0.08)
+    args = (0.0, 12.0, False, True, False)
+    img, _, _ = run_engine(api, sc.grid, args, skip_test=False)
+    ref = _oracle(api, sc.grid, args, skip_test=False).reshape(img.shape)
+    _check(img, ref, l2=2e-4, phase=None)
+    img_skip, _, _ = run_engine(api, sc.grid, args, skip_test=True)
+    ref_skip = _oracle(api, sc.grid, args, skip_test=True).reshape(img.shape)
+    _check(img_skip, ref_skip, l2=2e-4, phase=None)
+
+
+def test_parity_fp64_positions_and_grid(cuda_device):
+    """Jittered FP64 trajectory and FP64 grid (the precision-study inputs)."""
+    sc = scenes.small_scene(seed=21, n_pri=512, n_samples=256, nx=24, ny=24, jitter=0.5e-3, spacing=1e-3,
+                            y0=0.6, rail_len=1.0, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, INF, False, False, True)
+    img, stats, _ = run_engine(api, sc.grid, args, pos64=sc.positions, grid64=sc.grid)
+    assert stats["path_name"] == "fp32_bulk"
+    ref = _oracle(api, sc.grid, args, pos64=sc.positions, grid64=True).reshape(img.shape)
+    _check(img, ref)
+    assert peak_err(img, ref) < 1e-5
+
+
+def test_fp64_phase_comparator(cuda_device):
+    sc = scenes.small_scene(seed=22, n_pri=256, n_samples=128, nx=20, ny=20, jitter=0.3e-3, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, INF, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args, pos64=sc.positions, grid64=sc.grid, precision="fp64")
+    assert stats["path_name"] == "fp64_phase"
+    ref = _oracle(api, sc.grid, args, pos64=sc.positions, grid64=True).reshape(img.shape)
+    _check(img, ref)
+
+
+def test_general_path_per_sample_trajectory(cuda_device):
+    """position[c, s] varies within the chirp (tdckernels.cu:204-208 reads it per element)."""
+    sc = scenes.small_scene(seed=23, n_pri=192, n_samples=64, nx=14, ny=12, device="cuda")
+    api = sc.api_arrays()
+    C, S = sc.n_pri, sc.n_samples
+    pos = api["position"].astype(np.float64)
+    pos[..., 0] += (np.arange(S) / S * 0.4e-3)[None, :]       # antenna keeps moving during the chirp
+    api["position"] = pos.astype(np.float32)
+    api["velocity"] = np.zeros((C, S, 3), np.float32)
+    api["velocity"][..., 0] = 0.02
+    args = (0.0, 40.0, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "general"
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref, l2=2e-4, phase=None)
+
+
+def test_general_path_nonuniform_sample_times(cuda_device):
+    sc = scenes.small_scene(seed=24, n_pri=128, n_samples=96, nx=12, ny=10, device="cuda")
+    api = sc.api_arrays()
+    rng = np.random.default_rng(3)
+    st = api["sampleTimes"].astype(np.float64)
+    st = st + rng.uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
+    api["sampleTimes"] = st.astype(np.float32)
+    args = (0.0, INF, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "general"
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref)
+
+
+def test_repeatable_and_linear(cuda_device):
+    sc = scenes.small_scene(seed=31, n_pri=256, n_samples=64, nx=16, ny=16, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, INF, False, True, True)
+    a, _, _ = run_engine(api, sc.grid, args)
+    b, _, _ = run_engine(api, sc.grid, args)
+    np.testing.assert_array_equal(a, b)
+    api2 = dict(api)
+    api2["rawData"] = (api["rawData"] * np.float32(2.0)).astype(np.complex64)
+    c, _, _ = run_engine(api2, sc.grid, args)
+    np.testing.assert_array_equal(c, 2 * a)          # scaling by 2 is exact through every FP32 step
+
+
+def test_processor_reuse_and_reference_call_order(cuda_device):
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=41, n_pri=128, n_samples=32, nx=8, ny=8, device="cuda")
+    api = sc.api_arrays()
+    p = _sarlabtdc.TdcProcessor(0)
+    with pytest.raises(RuntimeError):
+        p.start(0.0, INF, False, True)              # before setRawData / setFocusGrid
+    p.setRawData(*api.values())
+    with pytest.raises(RuntimeError):
+        p.start(0.0, INF, False, True)
+    p.setFocusGrid(sc.grid)
+    p.start(0.0, INF, False, True)
+    first = p.getFocusedImage()
+    assert first.shape == (8, 8) and first.dtype == np.complex64
+    first[...] = 0                                   # getFocusedImage returns a copy
+    p.start(0.0, INF, False, True)
+    again = p.getFocusedImage()
+    assert np.abs(again).max() > 0
+    smaller = sc.grid[:3, :5]
+    p.setFocusGrid(smaller)
+    p.start(0.0, INF, False, True)
+    assert p.getFocusedImage().shape == (3, 5)
+    np.testing.assert_array_equal(p.getFocusedImage(), again[:3, :5])
+    with pytest.raises(ValueError):
+        p.setRawData(np.zeros((0, 4), np.complex64), np.zeros(0, np.float32), np.zeros(4, np.float32),
+                     np.zeros((0, 4, 3), np.float32), np.zeros((0, 4, 3), np.float32),
+                     np.zeros((0, 4, 4), np.float32), 1.0, 1.0, np.zeros(3, np.float32))
+
+
+def test_device_resident_focus_matches_start(cuda_device):
+    import torch
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=51, n_pri=256, n_samples=64, nx=20, ny=18, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, INF, False, True, True)
+    img, _, p = run_engine(api, sc.grid, args)
+    p.prepare(*args)
+    p.uploadGrid()
+    out = torch.empty(p.numPixels(), dtype=torch.complex64, device="cuda")
+    p.focusDevice(out)
+    p.check()
+    np.testing.assert_array_equal(out.cpu().numpy().reshape(img.shape), img)
+    # on a torch stream
+    s = torch.cuda.Stream()
+    out2 = torch.zeros_like(out)
+    p.focusDevice(out2, stream=s)
+    p.check(stream=s)
+    np.testing.assert_array_equal(out2.cpu().numpy().reshape(img.shape), img)
