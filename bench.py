@@ -193,7 +193,7 @@ def fp32_peak_tflops(lib, torch):
     for _ in range(5):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        rc = lib.tdc_probe_fma(0, n_sm * 8, 4000, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
+        rc = lib.tdc_probe_fma(0, n_sm * 8, 1000, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
         assert rc == 0
@@ -202,7 +202,7 @@ def fp32_peak_tflops(lib, torch):
     for _ in range(2):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        lib.tdc_probe_fma(1, n_sm * 2, 200, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
+        lib.tdc_probe_fma(1, n_sm * 2, 25, scratch.data_ptr(), C.byref(flops), stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
         fp64 = max(fp64, flops.value / (e0.elapsed_time(e1) / 1e3) / 1e12)

@@ -166,12 +166,12 @@ int tdc_processor_upload_grid(tdc_processor *proc);
  * correlateAndSum launches of tdcprocessor.cpp:82-144, and sumScratchSize):
  * image_dev[p] (complex float, interleaved) for every pixel of the resident
  * grid, from the resident acquisition. Asynchronous on `stream` (NULL = the
- * processor's stream); the processor owns the scratch memory. Call
+ * legacy default stream); the processor owns the scratch memory. Call
  * tdc_processor_check before reading results to collect device-side errors.
  */
 int tdc_processor_focus_device(tdc_processor *proc, float *image_dev, void *stream);
 
-/* Synchronise `stream` (NULL = the processor's) and report a kernel-side error
+/* Synchronise `stream` (NULL = the legacy default stream) and report a kernel-side error
  * (TDC_ERR_TIMEOUT when a bounded wait expired). */
 int tdc_processor_check(tdc_processor *proc, void *stream);
 
@@ -183,7 +183,7 @@ int tdc_processor_path(const tdc_processor *proc);
 
 /* ---- measurement helper (no reference counterpart) ---- */
 
-/* FMA throughput probe: blocks x 256 threads x iters x 16 FMAs, FP32 (fp64 = 0)
+/* FMA throughput probe: blocks x 256 threads x iters x 128 FMAs, FP32 (fp64 = 0)
  * or FP64. *flops receives the FLOP count (2 per FMA); the caller times the
  * launch with events on `stream`. scratch_dev: >= blocks x 8 bytes (never written
  * in practice). */

@@ -174,17 +174,22 @@ class TdcProcessor:
     def path(self) -> str:
         return _lib.PATH_NAMES.get(_lib.lib().tdc_processor_path(self._h), "none")
 
+    @staticmethod
+    def _stream(stream):
+        """A CUDA stream handle: an int, a torch stream, or None for torch's current stream."""
+        if stream is None:
+            import torch
+
+            stream = torch.cuda.current_stream()
+        return stream if isinstance(stream, int) else stream.cuda_stream
+
     def focusDevice(self, image, stream=None):
         """Focus the resident acquisition onto the resident grid into ``image``
-        (a complex64 CUDA tensor of numPixels() elements, or a device address)."""
+        (a complex64 CUDA tensor of numPixels() elements, or a device address),
+        asynchronously on ``stream`` (default: torch's current stream)."""
         addr = image if isinstance(image, int) else image.data_ptr()
-        st = None
-        if stream is not None:
-            st = stream if isinstance(stream, int) else stream.cuda_stream
-        _lib.check(_lib.lib().tdc_processor_focus_device(self._h, addr, st))
+        _lib.check(_lib.lib().tdc_processor_focus_device(self._h, addr, self._stream(stream)))
 
     def check(self, stream=None):
-        st = None
-        if stream is not None:
-            st = stream if isinstance(stream, int) else stream.cuda_stream
-        _lib.check(_lib.lib().tdc_processor_check(self._h, st))
+        """Synchronise ``stream`` and raise if a focus kernel reported an error."""
+        _lib.check(_lib.lib().tdc_processor_check(self._h, self._stream(stream)))

@@ -863,14 +863,15 @@ int tdc_processor_focus_device(tdc_processor *p, float *image_dev, void *stream)
     if (!image_dev && p->P > 0) return fail(TDC_ERR_INVALID_ARGUMENT, "null image");
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
     int launches = 0;
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+    // NULL is the legacy default stream (torch's default stream), as for any CUDA API.
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     return focus_resident(p, reinterpret_cast<float2 *>(image_dev), st, launches);
 }
 
 int tdc_processor_check(tdc_processor *p, void *stream)
 {
     if (int rc = check_proc(p)) return rc;
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     TDC_CK(cudaStreamSynchronize(st), "focus sync");
     if (p->scratch.p) return read_status(p);
     return TDC_OK;

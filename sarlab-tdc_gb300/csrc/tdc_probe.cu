@@ -17,9 +17,13 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(int iters, T seed, T *__
 #pragma unroll
     for (int k = 0; k < kChains; ++k) a[k] = seed + (T)(threadIdx.x + k);
     const T m = (T)0.999999, c = (T)1e-7;
+#pragma unroll 1
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int k = 0; k < kChains; ++k) a[k] = a[k] * m + c;
+        for (int r = 0; r < 8; ++r) {
+#pragma unroll
+            for (int k = 0; k < kChains; ++k) a[k] = a[k] * m + c;
+        }
     }
     T s = 0;
 #pragma unroll
@@ -31,7 +35,7 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(int iters, T seed, T *__
 
 extern "C" {
 
-// Launch `blocks` x 256 threads of `iters` x 16 FMAs (FP32 when fp64 == 0, else FP64).
+// Launch `blocks` x 256 threads of `iters` x 128 FMAs (FP32 when fp64 == 0, else FP64).
 // Returns the FLOP count (2 per FMA) through *flops. Time it with events on `stream`.
 int tdc_probe_fma(int fp64, int blocks, int iters, void *scratch_dev, double *flops, void *stream)
 {
@@ -42,7 +46,7 @@ int tdc_probe_fma(int fp64, int blocks, int iters, void *scratch_dev, double *fl
     } else {
         fma_probe_kernel<float><<<blocks, 256, 0, st>>>(iters, 1.0f, static_cast<float *>(scratch_dev));
     }
-    if (flops) *flops = 2.0 * kChains * (double)iters * (double)blocks * 256.0;
+    if (flops) *flops = 2.0 * 8.0 * kChains * (double)iters * (double)blocks * 256.0;
     return cudaGetLastError() == cudaSuccess ? TDC_OK : TDC_ERR_CUDA;
 }
 

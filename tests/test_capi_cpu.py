@@ -15,7 +15,7 @@ def _declared_c_functions():
     names = set()
     for h in HEADERS:
         text = h.read_text()
-        if 'extern "C"' not in text and "tdc_" not in text:
+        if 'extern "C"' not in text:
             continue
         body = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         body = re.sub(r"//[^\n]*", "", body)
@@ -143,3 +143,19 @@ def test_no_closed_copy_calls_in_sources():
     pkg = ROOT / "sarlab-tdc_gb300" / "csrc"
     for f in pkg.iterdir():
         assert "BatchAsync" not in f.read_text()
+
+
+def _cpp_build(tmp_path):
+    exe = tmp_path / "tdcprocessor_smoke"
+    lib_dir = ROOT / "sarlab-tdc_gb300"
+    cmd = ["g++", "-std=c++17", "-O1", "-I", str(ROOT / "include"), "-I", "/usr/local/cuda/include",
+           str(ROOT / "tests" / "cpp" / "tdcprocessor_smoke.cpp"), "-L", str(lib_dir), "-ltdc_gb300",
+           f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_cpp_header_compiles_and_links(engine_lib, tmp_path):
+    """include/tdcprocessor.h is a drop-in for the reference's class: a tdctest-shaped program builds."""
+    assert _cpp_build(tmp_path).exists()

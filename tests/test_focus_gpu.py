@@ -245,3 +245,13 @@ def test_device_resident_focus_matches_start(cuda_device):
     p.focusDevice(out2, stream=s)
     p.check(stream=s)
     np.testing.assert_array_equal(out2.cpu().numpy().reshape(img.shape), img)
+
+
+def test_cpp_tdcprocessor_smoke(cuda_device, tmp_path):
+    """The tdctest-shaped C++ program runs against the engine."""
+    import subprocess
+
+    from test_capi_cpu import _cpp_build
+
+    r = subprocess.run([str(_cpp_build(tmp_path))], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
