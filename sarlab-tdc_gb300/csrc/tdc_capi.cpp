@@ -510,7 +510,7 @@ ScratchLayout scratch_layout(long long P, int n_units, int n_groups)
 int stage_bytes_for(int s_pad, int &cb)
 {
     const int row = s_pad * 8 + (int)sizeof(ChirpRec);
-    cb = std::max(1, 16640 / row);
+    cb = std::max(1, kFocusStageTarget / row);
     return (int)round_up((size_t)cb * row, 128);
 }
 
@@ -626,6 +626,8 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
 }
 
 }  // namespace
+
+int tdc::set_last_error(int code, const char *msg) { return fail(code, msg ? msg : ""); }
 
 // ===========================================================================
 // C ABI

@@ -6,6 +6,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace tdc {
 
 constexpr double kC0 = 299792458.0;  // SPEED_OF_LIGHT, tdcprocessor.cpp:37
@@ -13,12 +15,19 @@ constexpr int kChunk = 128;          // PRI_CHUNKSIZE, tuning.h:18
 constexpr float kRangeA = 25.0f / 46.0f;    // RANGE_WINDOW_A_PARAMETER, tuning.h:31
 constexpr float kAzimuthA = 25.0f / 46.0f;  // AZIMUTH_WINDOW_A_PARAMETER, tuning.h:38
 
-// Focus tile geometry of the FP32-bulk kernel: 128 threads x 4 pixels.
+// Focus tile geometry of the FP32-bulk kernel: 128 threads x TDC_FOCUS_PT pixels.
+#ifndef TDC_FOCUS_PT
+#define TDC_FOCUS_PT 4
+#endif
 constexpr int kFocusThreads = 128;
-constexpr int kFocusPT = 4;
+constexpr int kFocusPT = TDC_FOCUS_PT;
 constexpr int kFocusTile = kFocusThreads * kFocusPT;
 constexpr int kFocusStages = 3;
 constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows stay 128-byte sized)
+#ifndef TDC_FOCUS_STAGE_TARGET
+#define TDC_FOCUS_STAGE_TARGET 16640
+#endif
+constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp rows + records per pipeline stage
 
 // One chirp's trajectory record, 48 bytes (3 x float4):
 //   p_hi.xyz  antenna position, high float of a double-float pair; p_hi.w = Doppler window centre [Hz]
@@ -100,6 +109,10 @@ cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_d
                               int *status_dev, int per_sample, cudaStream_t st);
 cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image,
                                 cudaStream_t st);
+
+// Record `msg` as the calling thread's tdc_last_error() and return `code`.
+int set_last_error(int code, const char *msg);
+inline int set_last_error(int code, const std::string &msg) { return set_last_error(code, msg.c_str()); }
 
 // Occupancy of the FP32-bulk kernel at a given dynamic shared memory size.
 int focus_fp32_blocks_per_sm(int stage_bytes);
