@@ -189,6 +189,61 @@ int tdc_processor_path(const tdc_processor *proc);
  * in practice). */
 int tdc_probe_fma(int fp64, int blocks, int iters, void *scratch_dev, double *flops, void *stream);
 
+/* ---- focus without allocation (no counterpart in the reference) ---- */
+
+/*
+ * For callers that cannot allocate device memory while they focus: processing
+ * chains that provision all device memory once at start-up (real-time or
+ * certified radar pipelines with a fixed budget), plug-ins inside a host
+ * framework that owns the device allocator, code that must not call cudaMalloc
+ * during stream capture. tdc_focus_noalloc runs the same FP32-bulk focus as
+ * tdc_processor_focus_device on inputs and an output the caller owns; its
+ * scratch memory is a fixed array inside this library (TDC_NOALLOC_SCRATCH_BYTES
+ * on every GPU that loads the library, held until the process exits), so it
+ * calls no cudaMalloc / cudaFree. That limits the grid to about 2M pixels
+ * (larger grids return TDC_ERR_UNSUPPORTED before anything runs).
+ *
+ * All calls on a device share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race on it and must be serialised by the
+ * caller. The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture. Each call is blocking: it returns after the image is
+ * written and the kernels' status word has been read.
+ *
+ * Inputs (device pointers, 16-byte aligned):
+ *   samples      n_pri rows of s_pad complex floats (interleaved): the range-
+ *                windowed samples, zero from n_samples to s_pad, where s_pad is
+ *                n_samples rounded up to a multiple of 16
+ *   chirps       n_pri records of 12 floats: position (x, y, z) high floats,
+ *                Doppler window centre [Hz], position low floats (x, y, z)
+ *                (position = high + low, double-float), 0, velocity (x, y, z), 0
+ *   skip_points  ceil(n_pri / 128) x 9 points x 8 floats of the reference's chunk
+ *                skip test (position xyz, window centre, velocity xyz, 0), or
+ *                NULL to process every chunk
+ *   grid_hi      n_pix x 4 floats (x, y, z, 0); grid_lo the low floats or NULL
+ *   g0, g1       2 f(s) / c = g0 + s g1 [cycles per metre], f(s) the frequency of sample s
+ * Output: image_dev, n_pix complex floats (interleaved).
+ */
+#define TDC_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+typedef struct tdc_noalloc_focus_args {
+    const float *samples;
+    const float *chirps;
+    const float *skip_points;
+    const float *grid_hi;
+    const float *grid_lo;
+    int64_t n_pix;
+    int n_pri;
+    int n_samples;
+    double g0;
+    double g1;
+    float lambda;              /* centre wavelength, used by the Doppler window */
+    float doppler_bandwidth;   /* Hz; +inf for no Doppler windowing */
+    int doppler_win_taper;
+} tdc_noalloc_focus_args;
+
+int tdc_focus_noalloc(const tdc_noalloc_focus_args *args, float *image_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,28 @@ PRECISION_FP64_PHASE = 1
 PATH_NAMES = {0: "fp32_bulk", 1: "fp64_phase", 2: "general"}
 
 
+class NoallocFocusArgs(C.Structure):
+    """tdc_noalloc_focus_args of include/tdc_gb300.h."""
+    _fields_ = [
+        ("samples", C.c_void_p),
+        ("chirps", C.c_void_p),
+        ("skip_points", C.c_void_p),
+        ("grid_hi", C.c_void_p),
+        ("grid_lo", C.c_void_p),
+        ("n_pix", C.c_int64),
+        ("n_pri", C.c_int),
+        ("n_samples", C.c_int),
+        ("g0", C.c_double),
+        ("g1", C.c_double),
+        ("lambda_", C.c_float),
+        ("doppler_bandwidth", C.c_float),
+        ("doppler_win_taper", C.c_int),
+    ]
+
+
+NOALLOC_SCRATCH_BYTES = 32 << 20
+
+
 class StartStats(C.Structure):
     _fields_ = [
         ("h2d_ms", C.c_double),
@@ -76,6 +98,7 @@ SIGNATURES = [
     ("tdc_processor_num_pixels", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("tdc_processor_path", C.c_int, [_vp]),
     ("tdc_probe_fma", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.POINTER(C.c_double), _vp]),
+    ("tdc_focus_noalloc", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp]),
 ]
 
 _LIB = None

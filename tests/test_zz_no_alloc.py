@@ -1,0 +1,127 @@
+"""tdc_focus_noalloc: the focus entry point for callers that cannot allocate
+device memory (fixed-budget real-time chains, plug-ins inside a framework that
+owns the allocator, stream capture). Its scratch is a fixed array inside the
+library, so it must give the same image as tdc_processor_focus_device, call
+after call, with inputs the caller lays out itself as the header documents.
+
+This file is collected last on purpose (test_zz_*), so a stop-at-first-failure
+run has executed every other test before it."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tdc_testutil import max_phase_err, rel_l2, run_engine
+
+L2_TOL = 1e-4
+PHASE_TOL = 1e-3
+C0 = 299792458.0
+
+
+def _affine_fit(sample_times, mod_rate, start_freq):
+    """2 f_s / c = g0 + s g1, least squares on f_s = f0 + K t_s (the processor's fit)."""
+    t = np.asarray(sample_times, np.float32).astype(np.float64)
+    f = float(np.float32(start_freq)) + float(np.float32(mod_rate)) * t
+    S = t.size
+    if S == 1:
+        return 2 * f[0] / C0, 0.0
+    s = np.arange(S, dtype=np.float64)
+    sm, fm = 0.5 * (S - 1), f.mean()
+    F1 = np.sum((s - sm) * (f - fm)) / np.sum((s - sm) ** 2)
+    F0 = fm - F1 * sm
+    return 2 * F0 / C0, 2 * F1 / C0
+
+
+def _device_inputs(api, grid, torch):
+    """The documented device layout, built by the caller with its own memory."""
+    raw = api["rawData"]
+    n_pri, S = raw.shape
+    s_pad = (S + 15) // 16 * 16
+    samples = torch.zeros((n_pri, s_pad), dtype=torch.complex64, device="cuda")
+    samples[:, :S] = torch.from_numpy(np.ascontiguousarray(raw)).cuda()
+    rec = np.zeros((n_pri, 12), np.float32)
+    rec[:, 0:3] = api["position"][:, 0, :]
+    rec[:, 3] = 0.0                      # fixed Doppler window centre
+    rec[:, 8:11] = api["velocity"][:, 0, :]
+    chirps = torch.from_numpy(rec).cuda()
+    g = np.asarray(grid, np.float32).reshape(-1, 3)
+    gh = np.zeros((g.shape[0], 4), np.float32)
+    gh[:, :3] = g
+    grid_hi = torch.from_numpy(gh).cuda()
+    st = api["sampleTimes"]
+    chirp_t = float(np.float32(st[-1] - st[0]))
+    f0 = float(np.float32(api["startFreq"]))
+    centre = (f0 + (f0 + float(np.float32(api["modRate"])) * chirp_t)) / 2.0
+    lam = float(np.float32(C0 / centre))
+    g0, g1 = _affine_fit(st, api["modRate"], api["startFreq"])
+    return samples, chirps, grid_hi, g0, g1, lam
+
+
+@pytest.mark.gpu
+def test_noalloc_focus_matches_device_focus_twice_in_a_row(cuda_device):
+    import torch
+
+    import _tdc_capi
+    from sarlabtdc import scenes
+
+    lib = _tdc_capi.lib()
+    sc = scenes.small_scene(seed=61, n_pri=300, n_samples=100, nx=40, ny=30, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, float("inf"), False, False, True)
+    _, stats, p = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "fp32_bulk"
+    p.prepare(*args)
+    p.uploadGrid()
+    n_pix = p.numPixels()
+    ref = torch.empty(n_pix, dtype=torch.complex64, device="cuda")
+    p.focusDevice(ref)
+    p.check()
+    ref_np = ref.cpu().numpy()
+
+    samples, chirps, grid_hi, g0, g1, lam = _device_inputs(api, sc.grid, torch)
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = samples.data_ptr()
+    a.chirps = chirps.data_ptr()
+    a.skip_points = None
+    a.grid_hi = grid_hi.data_ptr()
+    a.grid_lo = None
+    a.n_pix = n_pix
+    a.n_pri = sc.n_pri
+    a.n_samples = sc.n_samples
+    a.g0, a.g1 = g0, g1
+    a.lambda_ = lam
+    a.doppler_bandwidth = float("inf")
+    a.doppler_win_taper = 1
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for _ in range(2):
+        out = torch.full((n_pix,), complex(float("nan"), 0.0), dtype=torch.complex64, device="cuda")
+        rc = lib.tdc_focus_noalloc(C.byref(a), C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+        assert rc == 0, _tdc_capi.last_error()
+        outs.append(out.cpu().numpy())
+    for o in outs:
+        assert np.all(np.isfinite(o))
+        assert rel_l2(o, ref_np) <= L2_TOL
+        assert max_phase_err(o, ref_np) <= PHASE_TOL
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_noalloc_rejects_grids_beyond_its_fixed_scratch():
+    """Size check only: returns before any CUDA call (run where no GPU is present)."""
+    import torch
+
+    import _tdc_capi
+
+    if torch.cuda.is_available():
+        pytest.skip("host-side rejection is checked where no GPU is present")
+    lib = _tdc_capi.lib()
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = a.chirps = a.grid_hi = 4096      # never dereferenced: rejected on size first
+    a.n_pix = (_tdc_capi.NOALLOC_SCRATCH_BYTES // 16) + 1
+    a.n_pri = 128
+    a.n_samples = 256
+    a.lambda_ = 0.0039
+    a.doppler_bandwidth = float("inf")
+    rc = lib.tdc_focus_noalloc(C.byref(a), C.c_void_p(4096), None)
+    assert rc == _tdc_capi.TDC_ERR_UNSUPPORTED
+    assert "bytes of scratch" in _tdc_capi.last_error()
