@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--side", type=int, default=1024, help="grid side (pixels)")
-    ap.add_argument("--chirps", type=int, default=4096)
-    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--config", default="2", choices=["1", "2", "3"],
+                    help="1: 256^2 stripmap, 1024 x 512; 2: precision study (default); 3: 3-D volume")
+    ap.add_argument("--side", type=int, default=1024, help="grid side (pixels), config 2")
+    ap.add_argument("--chirps", type=int, default=4096, help="config 2")
+    ap.add_argument("--samples", type=int, default=1024, help="config 2")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--quick", action="store_true", help="skip plain / e2e / CPU legs")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the oracle accuracy check")
@@ -121,11 +123,33 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
+WORKLOADS = {
+    "1": "plain stripmap: 256x256 px @2mm, 1024 chirps x 512 samples, 0.5 m rail, FP32 API inputs",
+    "3": "3-D volume: 256x256x64 voxels, 128x128 planar aperture @1mm, 256 samples, FP32 API inputs",
+}
+
+
+def uses_f64(args):
+    return args.config == "2"
+
+
+def workload(args, sc):
+    if args.config == "2":
+        return (f"precision study: {args.side}x{args.side} px @1mm, {sc.n_pri} chirps x {sc.n_samples} samples, "
+                "2 m jittered rail, FP64 positions + grid")
+    return WORKLOADS[args.config]
+
+
 def make_scene(args, device):
     from sarlabtdc import scenes
 
     t = time.time()
-    sc = scenes.config2(device=device, n_pix_side=args.side, n_pri=args.chirps, n_samples=args.samples)
+    if args.config == "1":
+        sc = scenes.config1(device=device)
+    elif args.config == "3":
+        sc = scenes.config3(device=device)
+    else:
+        sc = scenes.config2(device=device, n_pix_side=args.side, n_pri=args.chirps, n_samples=args.samples)
     log(f"scene: {sc.n_pix} px x {sc.n_pri} chirps x {sc.n_samples} samples "
         f"({sc.correlations() / 1e9:.1f} Gcorr) generated in {time.time() - t:.1f}s")
     return sc
@@ -139,11 +163,16 @@ def sample_pixels(sc, n_random, seed=0):
     return np.array(sorted(set(near + rnd)), dtype=np.int64)
 
 
-def oracle_problem(sc, api):
+def oracle_problem(sc, api, f64=True):
+    """The oracle on exactly the inputs the engine receives (FP64 trajectory and grid
+    through the extensions, or the FP32 API arrays)."""
     import oracle
 
-    return oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions,
-                          modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid)
+    if f64:
+        return oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions,
+                              modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid)
+    return oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=api["position"][:, 0, :],
+                          modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid.astype(np.float32))
 
 
 def oracle_opts():
@@ -153,12 +182,12 @@ def oracle_opts():
     return oracle.Opts(applyRangeWin=False, dopplerBandwidth=float("inf"))
 
 
-def time_oracle(sc, api, budget_s, threads):
+def time_oracle(sc, api, budget_s, threads, f64=True):
     """FP64 oracle throughput (Gcorr/s) on a bounded pixel sample sized to ~budget_s."""
     import oracle
 
     build_oracle()
-    prob = oracle_problem(sc, api)
+    prob = oracle_problem(sc, api, f64)
     o = oracle_opts()
     rng = np.random.default_rng(123)
     per_px = sc.n_pri * sc.n_samples
@@ -236,11 +265,19 @@ def run_ours(args):
     inf = float("inf")
     start_args = (0.0, inf, False, False, True)
 
+    f64 = uses_f64(args)
+
+    def load(proc, grid):
+        proc.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                        api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+        if f64:
+            proc.setChirpPositionsF64(sc.positions)
+            proc.setFocusGridF64(grid)
+        else:
+            proc.setFocusGrid(grid.astype(np.float32))
+
     p = _sarlabtdc.TdcProcessor(0)
-    p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
-                 api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
-    p.setChirpPositionsF64(sc.positions)
-    p.setFocusGridF64(sc.grid)
+    load(p, sc.grid)
     p.prepare(*start_args)
     p.uploadGrid()
     path = p.path()
@@ -290,8 +327,7 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
-           "config": {"workload": f"precision study: {args.side}x{args.side} px @1mm, {Cn} chirps x {S} samples, "
-                                  "2 m jittered rail, FP64 positions + grid",
+           "config": {"workload": workload(args, sc),
                       "pixels": P, "chirps": Cn, "samples": S, "correlations_per_step": corr,
                       "l2": "256 MiB buffer written between timed steps", "path": path},
            "latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 3),
@@ -307,7 +343,7 @@ def run_ours(args):
     build_oracle()
     pix = sample_pixels(sc, 192)
     t = time.time()
-    ref = oracle.focus(oracle_problem(sc, api), oracle_opts(), pixels=pix)
+    ref = oracle.focus(oracle_problem(sc, api, f64), oracle_opts(), pixels=pix)
     got = image[pix]
     sel = np.abs(ref) >= np.abs(ref).max() * 1e-2
     acc = {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
@@ -321,11 +357,8 @@ def run_ours(args):
         # plain all-FP64-phase comparator on a row band of the same grid
         rows = max(8, min(args.side, 64))
         q = _sarlabtdc.TdcProcessor(0)
-        q.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
-                     api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
-        q.setChirpPositionsF64(sc.positions)
         band = np.ascontiguousarray(sc.grid[:rows])
-        q.setFocusGridF64(band)
+        load(q, band)
         q.setPrecision("fp64")
         q.prepare(*start_args)
         q.uploadGrid()
@@ -343,7 +376,7 @@ def run_ours(args):
         band_pix = pix[pix < pim.size]
         plain_acc = None
         if band_pix.size:
-            rb = oracle.focus(oracle_problem(sc, api), oracle_opts(), pixels=band_pix)
+            rb = oracle.focus(oracle_problem(sc, api, f64), oracle_opts(), pixels=band_pix)
             plain_acc = float(np.linalg.norm(pim[band_pix] - rb) / np.linalg.norm(rb))
         out["plain"] = {"value": round(plain_gcorr, 2), "unit": UNIT, "speedup": round(kernel_gcorr / plain_gcorr, 2),
                         "rows": rows, "rel_l2": plain_acc, "kernel": "focus_fp64_kernel"}
@@ -355,10 +388,7 @@ def run_ours(args):
         times, stats = [], None
         for i in range(1 + e2e_steps):
             t = time.perf_counter()
-            p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
-                         api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
-            p.setChirpPositionsF64(sc.positions)
-            p.setFocusGridF64(sc.grid)
+            load(p, sc.grid)
             p.start(*start_args)
             host_img = p.getFocusedImage()
             dt = time.perf_counter() - t
@@ -375,7 +405,7 @@ def run_ours(args):
         assert np.array_equal(host_img.ravel(), image), "e2e image differs from the device-resident image"
         log(f"e2e {out['e2e']}")
 
-        cpu_g, npx, dt = time_oracle(sc, api, args.cpu_seconds, os.cpu_count())
+        cpu_g, npx, dt = time_oracle(sc, api, args.cpu_seconds, os.cpu_count(), f64)
         out["cpu_baseline"] = {"value": round(cpu_g, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{npx} random pixels x {Cn} chirps x {S} samples ({dt:.1f}s), "
                                          "FP64 OpenMP oracle loop"}
@@ -395,7 +425,7 @@ def run_reference(args):
     cores = os.cpu_count()
     import oracle
 
-    prob = oracle_problem(sc, api)
+    prob = oracle_problem(sc, api, uses_f64(args))
     o = oracle_opts()
     rng = np.random.default_rng(99)
     per_px = sc.n_pri * sc.n_samples
@@ -418,8 +448,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(times)), 2), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
            "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
-           "config": {"workload": f"precision study: {args.side}x{args.side} px @1mm, {sc.n_pri} chirps x "
-                                  f"{sc.n_samples} samples, 2 m jittered rail, FP64 positions + grid",
+           "config": {"workload": workload(args, sc),
                       "pixels": sc.n_pix, "chirps": sc.n_pri, "samples": sc.n_samples},
            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
                             "sample": f"{npx} random pixels per step x {sc.n_pri} chirps x {sc.n_samples} samples; "

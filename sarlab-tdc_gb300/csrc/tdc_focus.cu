@@ -39,9 +39,6 @@ namespace {
 #ifndef TDC_FOCUS_MINB
 #define TDC_FOCUS_MINB 3
 #endif
-#ifndef TDC_FOCUS_KMAJOR
-#define TDC_FOCUS_KMAJOR 0
-#endif
 constexpr int kL = TDC_FOCUS_L;  // in-block phasor table length
 
 struct SharedPixel {
@@ -71,37 +68,6 @@ __device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2
         ti = fmaf(xi, p[k - 1].x, ti);
     }
     return make_float2(tr, ti);
-}
-
-// All PT pixels of one Horner block, sample-major: the FFMAs that share a sample
-// are issued back to back.
-__device__ __forceinline__ void horner_block_all(float2 (&h)[kFocusPT], const float2 (&ql)[kFocusPT],
-                                                 const float2 (&p)[kFocusPT][kL - 1], const float4 (&xv)[kL / 2])
-{
-    float tr[kFocusPT], ti[kFocusPT];
-#pragma unroll
-    for (int i = 0; i < kFocusPT; ++i) tr[i] = fmaf(h[i].x, ql[i].x, xv[0].x);
-#pragma unroll
-    for (int i = 0; i < kFocusPT; ++i) ti[i] = fmaf(h[i].x, ql[i].y, xv[0].y);
-#pragma unroll
-    for (int i = 0; i < kFocusPT; ++i) tr[i] = fmaf(-h[i].y, ql[i].y, tr[i]);
-#pragma unroll
-    for (int i = 0; i < kFocusPT; ++i) ti[i] = fmaf(h[i].y, ql[i].x, ti[i]);
-#pragma unroll
-    for (int k = 1; k < kL; ++k) {
-        const float xr = (k & 1) ? xv[k >> 1].z : xv[k >> 1].x;
-        const float xi = (k & 1) ? xv[k >> 1].w : xv[k >> 1].y;
-#pragma unroll
-        for (int i = 0; i < kFocusPT; ++i) tr[i] = fmaf(xr, p[i][k - 1].x, tr[i]);
-#pragma unroll
-        for (int i = 0; i < kFocusPT; ++i) ti[i] = fmaf(xr, p[i][k - 1].y, ti[i]);
-#pragma unroll
-        for (int i = 0; i < kFocusPT; ++i) tr[i] = fmaf(-xi, p[i][k - 1].y, tr[i]);
-#pragma unroll
-        for (int i = 0; i < kFocusPT; ++i) ti[i] = fmaf(xi, p[i][k - 1].x, ti[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < kFocusPT; ++i) h[i] = make_float2(tr[i], ti[i]);
 }
 
 __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
@@ -277,12 +243,8 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     float4 xv[kL / 2];
 #pragma unroll
                     for (int m = 0; m < kL / 2; ++m) xv[m] = xs[b * (kL / 2) + m];
-#if TDC_FOCUS_KMAJOR
-                    horner_block_all(h, ql, p, xv);
-#else
 #pragma unroll
                     for (int i = 0; i < kFocusPT; ++i) h[i] = horner_block(h[i], ql[i], p[i], xv);
-#endif
                 }
 
 #pragma unroll
