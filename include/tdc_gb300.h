@@ -105,6 +105,13 @@ int tdc_processor_grid_shape(const tdc_processor *proc, int *n_rows, int *n_cols
  * tolerance. Borrowed like the other inputs. NULL clears the override. */
 int tdc_processor_set_chirp_positions_f64(tdc_processor *proc, const double *position_f64, int n_pri);
 
+/* Per-chirp trajectory (ingest extension): position n_pri x 3, velocity n_pri x 3
+ * or NULL (zero), attitude n_pri x 4 or NULL (identity), replacing the
+ * per-sample arrays of setRawData (40 bytes per sample) for antennas that do
+ * not move within a chirp. Borrowed like the other inputs. */
+int tdc_processor_set_trajectory_per_chirp(tdc_processor *proc, const float *position, const float *velocity,
+                                           const float *attitude);
+
 /* FP64 focus grid (n_rows x n_cols x 3), used instead of the FP32 grid. */
 int tdc_processor_set_focus_grid_f64(tdc_processor *proc, const double *focus_grid, int n_rows, int n_cols);
 
@@ -180,6 +187,91 @@ int tdc_processor_num_pixels(const tdc_processor *proc, int64_t *n_pix);
 
 /* tdc_path the next focus will take, or -1 when nothing is resident. */
 int tdc_processor_path(const tdc_processor *proc);
+
+/* ---- autofocus (no reference counterpart) ---- */
+
+/* Antenna positions of the resident acquisition := base + offsets_dev[c] (device,
+ * n_pri x 3 doubles, metres), base = the positions given to setRawData /
+ * setChirpPositionsF64; NULL restores the base. Needs a per-chirp trajectory.
+ * Asynchronous on `stream`. */
+int tdc_processor_set_chirp_offsets_device(tdc_processor *proc, const double *offsets_dev, void *stream);
+
+/*
+ * Adjoint of tdc_processor_focus_device with respect to the per-chirp position
+ * offsets: grad_offsets_dev[c] (n_pri x 3 doubles) = sum over pixels of
+ * Re(conj(G_p) dI_p/dR_pc) (P_c - T_p) / R_pc, with G = grad_image_dev
+ * (n_pix complex floats, dL/dRe I + j dL/dIm I, as torch stores the gradient
+ * of a complex tensor). The Doppler window and skip test are held fixed. The
+ * reference response is recomputed, not stored. Blocking. FP32-bulk path only.
+ */
+int tdc_processor_adjoint_device(tdc_processor *proc, const float *grad_image_dev, double *grad_offsets_dev,
+                                 void *stream);
+
+/* ---- request loop (no reference counterpart) ---- */
+
+/*
+ * A persistent request loop on one GPU: jobs submitted from any host thread are
+ * admitted while a processor slot is free and their device footprint fits in
+ * the memory budget next to the resident jobs (first come, first admitted);
+ * every focus launch carries work units of all admitted jobs (continuous
+ * batching, work split evenly between them). A job's image is bitwise the same
+ * whether it ran alone or in a mix.
+ */
+typedef struct tdc_server tdc_server;
+
+typedef struct tdc_job_desc {
+    const float *raw_iq;         /* n_pri x n_samples complex floats */
+    const float *sample_times;   /* n_samples */
+    const float *position;       /* n_pri x 3 per-chirp positions, or NULL when position_f64 is set */
+    const double *position_f64;  /* n_pri x 3 FP64 per-chirp positions for range and phase, or NULL */
+    const float *velocity;       /* n_pri x 3, or NULL (zero) */
+    const float *attitude;       /* n_pri x 4, or NULL (identity) */
+    int n_pri;
+    int n_samples;
+    float mod_rate;
+    float start_freq;
+    float body_boresight[3];
+    const float *grid;           /* n_pix x 3, or NULL when grid_f64 is set */
+    const double *grid_f64;      /* n_pix x 3, or NULL */
+    int64_t n_pix;
+    float doppler_win_center;    /* start() arguments */
+    float doppler_bandwidth;
+    int dop_centroid_win;
+    int apply_range_win;
+    int doppler_win_taper;
+    float *image;                /* n_pix complex floats, written before the job reports done */
+} tdc_job_desc;
+
+typedef struct tdc_job_info {
+    double submit_ms;        /* times since the server started */
+    double admit_ms;
+    double first_launch_ms;
+    double done_ms;
+    int64_t correlations;
+    int status;              /* tdc_status of the job */
+    int path;                /* tdc_path */
+} tdc_job_info;
+
+typedef struct tdc_server_stats {
+    int64_t jobs_submitted;
+    int64_t jobs_done;
+    int64_t jobs_failed;
+    int64_t launches;
+    int64_t correlations;
+    int64_t device_bytes_in_use;
+    int queued;
+    int active;
+} tdc_server_stats;
+
+/* memory_budget_bytes = 0: half of the free device memory; max_jobs = 0: 8. */
+int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_server **out);
+/* Inputs are borrowed until the job is done. */
+int tdc_server_submit(tdc_server *srv, const tdc_job_desc *job, uint64_t *job_id);
+/* Wait up to timeout_ms (< 0: forever); TDC_ERR_TIMEOUT if not finished. Returns the job's status. */
+int tdc_server_wait(tdc_server *srv, uint64_t job_id, int timeout_ms, tdc_job_info *info);
+int tdc_server_stats_get(tdc_server *srv, tdc_server_stats *out);
+/* Finishes the submitted jobs, then releases the server. */
+int tdc_server_destroy(tdc_server *srv);
 
 /* ---- measurement helper (no reference counterpart) ---- */
 

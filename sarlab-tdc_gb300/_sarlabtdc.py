@@ -133,6 +133,20 @@ class TdcProcessor:
         self._pos64_ref = pos
         _lib.check(_lib.lib().tdc_processor_set_chirp_positions_f64(self._h, _lib.ptr(pos), int(pos.shape[0])))
 
+    def setTrajectoryPerChirp(self, position, velocity=None, attitude=None):
+        """Per-chirp trajectory [nPri, 3] / [nPri, 3] / [nPri, 4] (FP32) replacing setRawData's
+        per-sample arrays; velocity and attitude default to zero and identity."""
+        pos = _arr(position, np.float32)
+        vel = None if velocity is None else _arr(velocity, np.float32)
+        att = None if attitude is None else _arr(attitude, np.float32)
+        n = self.numChirps()
+        if pos.shape != (n, 3) or (vel is not None and vel.shape != (n, 3)) or \
+                (att is not None and att.shape != (n, 4)):
+            raise RuntimeError("trajectory shape is incorrect")
+        self._traj_refs = (pos, vel, att)
+        _lib.check(_lib.lib().tdc_processor_set_trajectory_per_chirp(self._h, _lib.ptr(pos), _lib.ptr(vel),
+                                                                     _lib.ptr(att)))
+
     def setFocusGridF64(self, focusGrid):
         grid = np.ascontiguousarray(np.asarray(focusGrid, dtype=np.float64))
         if grid.ndim != 3:
@@ -166,6 +180,9 @@ class TdcProcessor:
     def uploadGrid(self):
         _lib.check(_lib.lib().tdc_processor_upload_grid(self._h))
 
+    def numChirps(self) -> int:
+        return int(self._raw_refs[0].shape[0]) if self._raw_refs else 0
+
     def numPixels(self) -> int:
         n = C.c_int64()
         _lib.check(_lib.lib().tdc_processor_num_pixels(self._h, C.byref(n)))
@@ -189,6 +206,18 @@ class TdcProcessor:
         asynchronously on ``stream`` (default: torch's current stream)."""
         addr = image if isinstance(image, int) else image.data_ptr()
         _lib.check(_lib.lib().tdc_processor_focus_device(self._h, addr, self._stream(stream)))
+
+    def setChirpOffsetsDevice(self, offsets, stream=None):
+        """Antenna positions := base + offsets (a CUDA float64 tensor [nPri, 3] or None)."""
+        addr = None if offsets is None else (offsets if isinstance(offsets, int) else offsets.data_ptr())
+        _lib.check(_lib.lib().tdc_processor_set_chirp_offsets_device(self._h, addr, self._stream(stream)))
+
+    def adjointDevice(self, grad_image, grad_offsets, stream=None):
+        """grad_offsets [nPri, 3] float64 (CUDA) <- adjoint of focusDevice applied to grad_image
+        (complex64 CUDA, dL/dRe I + j dL/dIm I). Blocking."""
+        gi = grad_image if isinstance(grad_image, int) else grad_image.data_ptr()
+        go = grad_offsets if isinstance(grad_offsets, int) else grad_offsets.data_ptr()
+        _lib.check(_lib.lib().tdc_processor_adjoint_device(self._h, gi, go, self._stream(stream)))
 
     def check(self, stream=None):
         """Synchronise ``stream`` and raise if a focus kernel reported an error."""

@@ -49,6 +49,63 @@ class NoallocFocusArgs(C.Structure):
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
+class JobDesc(C.Structure):
+    """tdc_job_desc of include/tdc_gb300.h."""
+    _fields_ = [
+        ("raw_iq", C.c_void_p),
+        ("sample_times", C.c_void_p),
+        ("position", C.c_void_p),
+        ("position_f64", C.c_void_p),
+        ("velocity", C.c_void_p),
+        ("attitude", C.c_void_p),
+        ("n_pri", C.c_int),
+        ("n_samples", C.c_int),
+        ("mod_rate", C.c_float),
+        ("start_freq", C.c_float),
+        ("body_boresight", C.c_float * 3),
+        ("grid", C.c_void_p),
+        ("grid_f64", C.c_void_p),
+        ("n_pix", C.c_int64),
+        ("doppler_win_center", C.c_float),
+        ("doppler_bandwidth", C.c_float),
+        ("dop_centroid_win", C.c_int),
+        ("apply_range_win", C.c_int),
+        ("doppler_win_taper", C.c_int),
+        ("image", C.c_void_p),
+    ]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [
+        ("submit_ms", C.c_double),
+        ("admit_ms", C.c_double),
+        ("first_launch_ms", C.c_double),
+        ("done_ms", C.c_double),
+        ("correlations", C.c_int64),
+        ("status", C.c_int),
+        ("path", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("jobs_submitted", C.c_int64),
+        ("jobs_done", C.c_int64),
+        ("jobs_failed", C.c_int64),
+        ("launches", C.c_int64),
+        ("correlations", C.c_int64),
+        ("device_bytes_in_use", C.c_int64),
+        ("queued", C.c_int),
+        ("active", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class StartStats(C.Structure):
     _fields_ = [
         ("h2d_ms", C.c_double),
@@ -88,6 +145,7 @@ SIGNATURES = [
     ("tdc_processor_set_chirp_positions_f64", C.c_int, [_vp, _vp, C.c_int]),
     ("tdc_processor_set_focus_grid_f64", C.c_int, [_vp, _vp, C.c_int, C.c_int]),
     ("tdc_processor_set_precision", C.c_int, [_vp, C.c_int]),
+    ("tdc_processor_set_trajectory_per_chirp", C.c_int, [_vp, _vp, _vp, _vp]),
     ("tdc_processor_last_stats", C.c_int, [_vp, C.POINTER(StartStats)]),
     ("tdc_range_window", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     ("tdc_processor_set_skip_test", C.c_int, [_vp, C.c_int]),
@@ -99,6 +157,13 @@ SIGNATURES = [
     ("tdc_processor_path", C.c_int, [_vp]),
     ("tdc_probe_fma", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.POINTER(C.c_double), _vp]),
     ("tdc_focus_noalloc", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp]),
+    ("tdc_processor_set_chirp_offsets_device", C.c_int, [_vp, _vp, _vp]),
+    ("tdc_processor_adjoint_device", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("tdc_server_create", C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(_vp)]),
+    ("tdc_server_submit", C.c_int, [_vp, C.POINTER(JobDesc), C.POINTER(C.c_uint64)]),
+    ("tdc_server_wait", C.c_int, [_vp, C.c_uint64, C.c_int, C.POINTER(JobInfo)]),
+    ("tdc_server_stats_get", C.c_int, [_vp, C.POINTER(ServerStats)]),
+    ("tdc_server_destroy", C.c_int, [_vp]),
 ]
 
 _LIB = None

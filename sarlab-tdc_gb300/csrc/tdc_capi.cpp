@@ -14,10 +14,12 @@
 
 #include "tdc_gb300.h"
 #include "tdc_internal.h"
+#include "tdc_processor_impl.h"
 
 using namespace tdc;
 
-namespace {
+namespace tdc {
+namespace impl {
 
 thread_local std::string g_err;
 
@@ -33,70 +35,9 @@ int cuda_fail(cudaError_t e, const char *what)
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define TDC_CK(call, what)                           \
-    do {                                             \
-        cudaError_t e_ = (call);                     \
-        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-    } while (0)
 
-// Grow-only device buffer.
-struct DevBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    cudaError_t ensure(size_t bytes)
-    {
-        if (bytes == 0) bytes = 16;
-        if (bytes <= cap) return cudaSuccess;
-        release();
-        cudaError_t e = cudaMalloc(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
-        else p = nullptr;
-        return e;
-    }
-    template <class T>
-    T *as() const
-    {
-        return static_cast<T *>(p);
-    }
-};
 
-// Grow-only pinned host buffer.
-struct PinnedBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    PinnedBuf() = default;
-    PinnedBuf(const PinnedBuf &) = delete;
-    PinnedBuf &operator=(const PinnedBuf &) = delete;
-    ~PinnedBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-    }
-    cudaError_t ensure(size_t bytes)
-    {
-        if (bytes == 0) bytes = 16;
-        if (bytes <= cap) return cudaSuccess;
-        release();
-        cudaError_t e = cudaMallocHost(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
-        else p = nullptr;
-        return e;
-    }
-};
 
-size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // ---- host FP32 math with the reference's semantics (gpumath.h, windowing.h) ----
 // Quaternions (a, b, c, d) = (w, x, y, z).
@@ -134,88 +75,19 @@ float window_centre(const float *vel, const float *att, const float *bore, float
     return 2.0f / lambda * ((vel[0] * ant[0]) + (vel[1] * ant[1]) + (vel[2] * ant[2]));
 }
 
-struct StartOpts {
-    float center = 0.f;
-    float bw = 0.f;
-    int centroid = 0;
-    int range_win = 1;
-    int taper = 1;
-    int skip_test = 1;
-};
 
-void split_dd(double v, float &h, float &l)
-{
-    h = static_cast<float>(v);
-    l = static_cast<float>(v - static_cast<double>(h));
-}
 
 // Phase tolerance for treating the sample frequencies as affine in the sample index.
 constexpr double kUniformPhaseTolRad = 1e-4;
 
-}  // namespace
+}  // namespace impl
+}  // namespace tdc
 
-// ===========================================================================
-// Processor
-// ===========================================================================
+using namespace tdc::impl;
 
-struct tdc_processor {
-    int device = 0;
-    int n_sm = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
 
-    // Borrowed inputs (setRawData / setFocusGrid).
-    const float *raw = nullptr;
-    const float *pri_times = nullptr;
-    const float *sample_times = nullptr;
-    const float *pos = nullptr;
-    const float *vel = nullptr;
-    const float *att = nullptr;
-    const double *pos64 = nullptr;
-    int C = 0, S = 0;
-    float mod_rate = 0.f, start_freq = 0.f;
-    float bore[3] = {0.f, 0.f, 0.f};
-    float lambda = 0.f;
-    bool has_raw = false;
-
-    const float *grid = nullptr;
-    const double *grid64 = nullptr;
-    int rows = 0, cols = 0;
-    bool has_grid = false;
-
-    int precision = TDC_PRECISION_FP32_BULK;
-    int skip_test = 1;
-
-    // Prepared acquisition (device resident).
-    bool prepared = false;
-    StartOpts opts;
-    bool per_chirp = true;
-    double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
-    double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
-    int s_pad = 0, n_chunks = 0;
-    DevBuf xw, chirps, skip, gs, pos_base, wr, offsets;
-
-    // Device grid.
-    long long P = 0;
-    bool grid_lo_valid = false;
-    double grid_min[3] = {0, 0, 0}, grid_max[3] = {0, 0, 0};
-    DevBuf grid_stage, grid_hi, grid_lo;
-
-    // Focus plan cache + scratch.
-    DevBuf scratch;
-    std::vector<FocusUnit> units_host;
-    long long plan_P = -1;
-    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0;
-    bool plan_uploaded = false;
-
-    DevBuf image_dev;
-    PinnedBuf image_host;
-    bool image_valid = false;
-
-    tdc_start_stats stats{};
-};
-
-namespace {
+namespace tdc {
+namespace impl {
 
 int check_proc(const tdc_processor *p)
 {
@@ -282,8 +154,11 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
 
     // ---- host analysis ----
-    p->per_chirp = (p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
-                   rows_constant(p->att, C, S, 4);
+    // Trajectory element of (chirp c, sample s): per-sample arrays, or one row per chirp.
+    const bool tpc = p->traj_per_chirp;
+    auto ti = [tpc, S](long c, long s) -> size_t { return tpc ? (size_t)c : (size_t)c * S + s; };
+    p->per_chirp = tpc || ((p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
+                           rows_constant(p->att, C, S, 4));
     fit_frequencies(p->sample_times, S, p->start_freq, p->mod_rate, p->F0, p->F1, p->resid_hz);
     for (int k = 0; k < 3; ++k) {
         p->ant_min[k] = std::numeric_limits<double>::infinity();
@@ -292,7 +167,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     std::vector<double> base((size_t)C * 3);
     for (int c = 0; c < C; ++c) {
         for (int k = 0; k < 3; ++k) {
-            const double v = p->pos64 ? p->pos64[3 * (size_t)c + k] : (double)p->pos[(size_t)c * S * 3 + k];
+            const double v = p->pos64 ? p->pos64[3 * (size_t)c + k] : (double)p->pos[3 * ti(c, 0) + k];
             base[3 * (size_t)c + k] = v;
             p->ant_min[k] = std::min(p->ant_min[k], v);
             p->ant_max[k] = std::max(p->ant_max[k], v);
@@ -315,8 +190,9 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         const int ns = p->per_chirp ? 1 : S;
         for (int s = 0; s < ns; ++s) {
             const size_t e = (size_t)c * S + s;
-            const float *vl = p->vel ? p->vel + 3 * e : kZero3;
-            const float *at = p->att ? p->att + 4 * e : kQId;
+            const size_t te = ti(c, s);
+            const float *vl = p->vel ? p->vel + 3 * te : kZero3;
+            const float *at = p->att ? p->att + 4 * te : kQId;
             const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
             ChirpRec r;
             float h[3], l[3];
@@ -324,7 +200,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                 if (p->pos64) {
                     split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
                 } else {
-                    h[k] = p->pos[3 * e + k];
+                    h[k] = p->pos[3 * te + k];
                     l[k] = 0.f;
                 }
             }
@@ -360,7 +236,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                         sp.pos_fdc = make_float4(0.f, 0.f, 0.f, fdc);
                         sp.vel = make_float4(0.f, 0.f, 0.f, 0.f);
                     } else {
-                        const size_t e = (size_t)pri * S + samples[j];
+                        const size_t e = ti(pri, samples[j]);
                         const float *ps = p->pos + 3 * e;
                         const float *vl = p->vel ? p->vel + 3 * e : kZero3;
                         const float *at = p->att ? p->att + 4 * e : kQId;
@@ -514,8 +390,40 @@ int stage_bytes_for(int s_pad, int &cb)
     return (int)round_up((size_t)cb * row, 128);
 }
 
-// Focus the resident acquisition onto the resident grid: image_dev (complex float [P]).
-int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &launches)
+// Job record of the resident acquisition x resident grid under the current plan.
+FocusJob make_job(const tdc_processor *p, float4 *partial, int cb)
+{
+    FocusJob job;
+    std::memset(&job, 0, sizeof(job));
+    job.xw = p->xw.as<const float4>();
+    job.chirps = p->chirps.as<const ChirpRec>();
+    job.grid_hi = p->grid_hi.as<const float4>();
+    job.grid_lo = p->grid_lo_valid ? p->grid_lo.as<const float4>() : nullptr;
+    job.skip = p->skip.as<const SkipPoint>();
+    job.gs = p->gs.as<const double>();
+    job.partial = partial;
+    job.P = p->P;
+    job.C = p->C;
+    job.S = p->S;
+    job.s_pad = p->s_pad;
+    job.n_groups = p->plan_groups;
+    job.chirps_per_group = p->plan_cpg;
+    job.chunk = kChunk;
+    job.stage_chirps = cb;
+    job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
+    job.n_tiles = (int)((p->P + kFocusTile - 1) / kFocusTile);
+    job.per_sample = p->per_chirp ? 0 : 1;
+    const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
+    split_dd(g0, job.g0_hi, job.g0_lo);
+    split_dd(g1, job.g1, job.g1_lo);
+    job.two_over_lambda = 2.0f / p->lambda;
+    job.half_bw = p->opts.bw / 2.0f;
+    job.inv_bw = 1.0f / p->opts.bw;
+    job.az_a = kAzimuthA;
+    return job;
+}
+
+int focus_plan(tdc_processor *p, FocusPlan &plan)
 {
     if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
     if (p->P <= 0) return fail(TDC_ERR_STATE, "no focus grid");
@@ -554,34 +462,30 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
         p->plan_uploaded = false;
     }
     unsigned char *scr = p->scratch.as<unsigned char>();
+    plan.path = path;
+    plan.cb = cb;
+    plan.stage_bytes = stage_bytes;
+    plan.slots = slots;
+    plan.off_job = L.off_job;
+    plan.off_units = L.off_units;
+    plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb);
+    return TDC_OK;
+}
 
-    FocusJob job;
-    std::memset(&job, 0, sizeof(job));
-    job.xw = p->xw.as<const float4>();
-    job.chirps = p->chirps.as<const ChirpRec>();
-    job.grid_hi = p->grid_hi.as<const float4>();
-    job.grid_lo = p->grid_lo_valid ? p->grid_lo.as<const float4>() : nullptr;
-    job.skip = p->skip.as<const SkipPoint>();
-    job.gs = p->gs.as<const double>();
-    job.partial = reinterpret_cast<float4 *>(scr + L.off_partial);
-    job.P = P;
-    job.C = C;
-    job.S = p->S;
-    job.s_pad = p->s_pad;
-    job.n_groups = p->plan_groups;
-    job.chirps_per_group = p->plan_cpg;
-    job.chunk = kChunk;
-    job.stage_chirps = cb;
-    job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
-    job.n_tiles = (int)((P + kFocusTile - 1) / kFocusTile);
-    job.per_sample = p->per_chirp ? 0 : 1;
-    const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
-    split_dd(g0, job.g0_hi, job.g0_lo);
-    split_dd(g1, job.g1, job.g1_lo);
-    job.two_over_lambda = 2.0f / p->lambda;
-    job.half_bw = p->opts.bw / 2.0f;
-    job.inv_bw = 1.0f / p->opts.bw;
-    job.az_a = kAzimuthA;
+// Focus the resident acquisition onto the resident grid: image_dev (complex float [P]).
+int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &launches)
+{
+    FocusPlan plan;
+    if (int rc = focus_plan(p, plan)) return rc;
+    const long long P = p->P;
+    const int C = p->C;
+    const int path = plan.path, stage_bytes = plan.stage_bytes, slots = plan.slots;
+    const int n_units = (int)p->units_host.size();
+    unsigned char *scr = p->scratch.as<unsigned char>();
+    struct {
+        size_t off_job, off_units;
+    } L{plan.off_job, plan.off_units};
+    const FocusJob &job = plan.job;
 
     TDC_CK(cudaMemcpyAsync(scr + L.off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");
     if (!p->plan_uploaded) {
@@ -625,7 +529,8 @@ float elapsed(cudaEvent_t a, cudaEvent_t b)
     return ms;
 }
 
-}  // namespace
+}  // namespace impl
+}  // namespace tdc
 
 int tdc::set_last_error(int code, const char *msg) { return fail(code, msg ? msg : ""); }
 
@@ -700,6 +605,7 @@ int tdc_processor_set_raw_data(tdc_processor *p, const float *raw_iq, const floa
     const double centre = ((double)start_freq + end_freq) / 2.0;
     p->lambda = (float)(kC0 / centre);
     p->pos64 = nullptr;
+    p->traj_per_chirp = false;
     p->has_raw = true;
     p->prepared = false;
     return TDC_OK;
@@ -737,6 +643,20 @@ int tdc_processor_set_chirp_positions_f64(tdc_processor *p, const double *positi
     if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called first");
     if (position_f64 && n_pri != p->C) return fail(TDC_ERR_SHAPE, "position shape is incorrect");
     p->pos64 = position_f64;
+    p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_set_trajectory_per_chirp(tdc_processor *p, const float *position, const float *velocity,
+                                           const float *attitude)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called first");
+    if (!position) return fail(TDC_ERR_INVALID_ARGUMENT, "null position");
+    p->pos = position;
+    p->vel = velocity;
+    p->att = attitude;
+    p->traj_per_chirp = true;
     p->prepared = false;
     return TDC_OK;
 }
@@ -890,6 +810,75 @@ int tdc_processor_path(const tdc_processor *p)
 {
     if (!p || !p->prepared || p->P <= 0) return -1;
     return choose_path(p);
+}
+
+int tdc_processor_set_chirp_offsets_device(tdc_processor *p, const double *offsets_dev, void *stream)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
+    if (!p->per_chirp) return fail(TDC_ERR_UNSUPPORTED, "chirp offsets need a per-chirp trajectory");
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    TDC_CK(launch_chirp_positions(p->chirps.as<ChirpRec>(), p->pos_base.as<const double>(), offsets_dev, p->C,
+                                  static_cast<cudaStream_t>(stream)),
+           "chirp positions kernel");
+    return TDC_OK;
+}
+
+int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, double *grad_offsets_dev,
+                                 void *stream)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
+    if (p->P <= 0) return fail(TDC_ERR_STATE, "no focus grid");
+    if (!grad_image_dev || !grad_offsets_dev) return fail(TDC_ERR_INVALID_ARGUMENT, "null gradient buffer");
+    if (choose_path(p) != TDC_PATH_FP32_BULK)
+        return fail(TDC_ERR_UNSUPPORTED, "the adjoint needs the FP32-bulk path (per-chirp trajectory, uniform "
+                                         "sample spacing)");
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long P = p->P;
+    const int C = p->C;
+    int cb = 1;
+    const int stage_bytes = stage_bytes_for(p->s_pad, cb);
+    const int bps = adjoint_fp32_blocks_per_sm(stage_bytes, cb);
+    if (bps <= 0) return fail(TDC_ERR_CUDA, "adjoint kernel does not fit on the device");
+    const int slots = p->n_sm * bps;
+    int n_groups = 1, cpg = C;
+    plan_groups(P, C, slots, n_groups, cpg);
+    const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
+    std::vector<FocusUnit> units;
+    units.reserve((size_t)(n_tiles * n_groups));
+    for (long long t = 0; t < n_tiles; ++t)
+        for (int g = 0; g < n_groups; ++g) units.push_back(FocusUnit{0, (int)t, g, 0});
+    const size_t off_job = 256;
+    const size_t off_units = round_up(off_job + sizeof(FocusJob), 256);
+    const size_t off_gpart = round_up(off_units + units.size() * sizeof(FocusUnit), 256);
+    const size_t total = off_gpart + (size_t)n_tiles * C * 16;
+    TDC_CK(p->adj_scratch.ensure(total), "alloc adjoint scratch");
+    unsigned char *scr = p->adj_scratch.as<unsigned char>();
+    FocusJob job = make_job(p, nullptr, cb);
+    job.n_groups = n_groups;
+    job.chirps_per_group = cpg;
+    TDC_CK(cudaMemcpyAsync(scr + off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");
+    TDC_CK(cudaMemcpyAsync(scr + off_units, units.data(), units.size() * sizeof(FocusUnit), cudaMemcpyHostToDevice,
+                           st),
+           "copy units");
+    TDC_CK(cudaMemsetAsync(scr, 0, 8, st), "reset counter");
+    float4 *gpart = reinterpret_cast<float4 *>(scr + off_gpart);
+    const int grid = (int)std::min<long long>((long long)units.size(), slots);
+    TDC_CK(launch_adjoint_fp32(reinterpret_cast<const FocusJob *>(scr + off_job),
+                               reinterpret_cast<const FocusUnit *>(scr + off_units), (int)units.size(),
+                               reinterpret_cast<int *>(scr), reinterpret_cast<int *>(scr) + 1, stage_bytes, cb, grid,
+                               reinterpret_cast<const float2 *>(grad_image_dev), gpart, st),
+           "adjoint kernel");
+    TDC_CK(launch_adjoint_reduce(gpart, (int)n_tiles, C, grad_offsets_dev, st), "adjoint reduce kernel");
+    // The host copies above are from stack/vector memory: finish before they go out of scope,
+    // and collect the kernel's status word.
+    TDC_CK(cudaStreamSynchronize(st), "adjoint sync");
+    int status = 0;
+    TDC_CK(cudaMemcpy(&status, scr + sizeof(int), sizeof(int), cudaMemcpyDeviceToHost), "read status");
+    if (status & kStatusTimeout) return fail(TDC_ERR_TIMEOUT, "adjoint kernel wait timed out");
+    return TDC_OK;
 }
 
 int tdc_range_window(float *w_dev, int n_samples, int apply_range_win, void *stream)

@@ -110,6 +110,15 @@ cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_d
 cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image,
                                 cudaStream_t st);
 
+// Adjoint of the FP32-bulk focus w.r.t. per-chirp position offsets: per-(tile, chirp)
+// float4 partials, then an FP64 sum over tiles into grad[C][3].
+cudaError_t launch_adjoint_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
+                                int *status_dev, int stage_bytes, int stage_chirps, int grid_ctas,
+                                const float2 *gimg, float4 *gpart, cudaStream_t st);
+cudaError_t launch_adjoint_reduce(const float4 *gpart, int n_tiles, int C, double *grad, cudaStream_t st);
+int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps);
+int adjoint_fp32_smem_bytes(int stage_bytes, int stage_chirps);
+
 // Record `msg` as the calling thread's tdc_last_error() and return `code`.
 int set_last_error(int code, const char *msg);
 inline int set_last_error(int code, const std::string &msg) { return set_last_error(code, msg.c_str()); }

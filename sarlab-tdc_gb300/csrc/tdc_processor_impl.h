@@ -1,0 +1,188 @@
+// tdc_processor_impl.h -- internal definition of the processor (the state behind
+// the tdc_processor handle of include/tdc_gb300.h) and the host-side steps of a
+// focus, shared by the C ABI (tdc_capi.cpp) and the request loop (tdc_server.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tdc_gb300.h"
+#include "tdc_internal.h"
+
+namespace tdc {
+namespace impl {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        else p = nullptr;
+        return e;
+    }
+    template <class T>
+    T *as() const
+    {
+        return static_cast<T *>(p);
+    }
+};
+
+// Grow-only pinned host buffer.
+struct PinnedBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMallocHost(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        else p = nullptr;
+        return e;
+    }
+};
+
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+inline void split_dd(double v, float &h, float &l)
+{
+    h = static_cast<float>(v);
+    l = static_cast<float>(v - static_cast<double>(h));
+}
+
+struct StartOpts {
+    float center = 0.f;
+    float bw = 0.f;
+    int centroid = 0;
+    int range_win = 1;
+    int taper = 1;
+    int skip_test = 1;
+};
+
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define TDC_CK(call, what)                           \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+}  // namespace impl
+}  // namespace tdc
+
+struct tdc_processor {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    // Borrowed inputs (setRawData / setFocusGrid).
+    const float *raw = nullptr;
+    const float *pri_times = nullptr;
+    const float *sample_times = nullptr;
+    const float *pos = nullptr;
+    const float *vel = nullptr;
+    const float *att = nullptr;
+    const double *pos64 = nullptr;
+    bool traj_per_chirp = false;  // pos / vel / att hold one row per chirp instead of one per sample
+    int C = 0, S = 0;
+    float mod_rate = 0.f, start_freq = 0.f;
+    float bore[3] = {0.f, 0.f, 0.f};
+    float lambda = 0.f;
+    bool has_raw = false;
+
+    const float *grid = nullptr;
+    const double *grid64 = nullptr;
+    int rows = 0, cols = 0;
+    bool has_grid = false;
+
+    int precision = TDC_PRECISION_FP32_BULK;
+    int skip_test = 1;
+
+    // Prepared acquisition (device resident).
+    bool prepared = false;
+    tdc::impl::StartOpts opts;
+    bool per_chirp = true;
+    double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
+    double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
+    int s_pad = 0, n_chunks = 0;
+    tdc::impl::DevBuf xw, chirps, skip, gs, pos_base, wr, offsets;
+
+    // Device grid.
+    long long P = 0;
+    bool grid_lo_valid = false;
+    double grid_min[3] = {0, 0, 0}, grid_max[3] = {0, 0, 0};
+    tdc::impl::DevBuf grid_stage, grid_hi, grid_lo;
+
+    // Focus plan cache + scratch.
+    tdc::impl::DevBuf scratch;
+    std::vector<tdc::FocusUnit> units_host;
+    long long plan_P = -1;
+    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0;
+    bool plan_uploaded = false;
+
+    // Adjoint (autofocus) scratch.
+    tdc::impl::DevBuf adj_scratch;
+
+    tdc::impl::DevBuf image_dev;
+    tdc::impl::PinnedBuf image_host;
+    bool image_valid = false;
+
+    tdc_start_stats stats{};
+};
+
+namespace tdc {
+namespace impl {
+
+// Work plan of one focus of a processor's resident acquisition onto its resident grid.
+struct FocusPlan {
+    int path = 0;         // tdc_path
+    int cb = 1;           // chirps per pipeline stage
+    int stage_bytes = 0;  // bytes per pipeline stage
+    int slots = 0;        // resident CTAs of the kernel on the device
+    size_t off_job = 0;   // job record and unit table offsets in the processor's scratch
+    size_t off_units = 0;
+    FocusJob job{};       // partial -> the processor's scratch
+};
+
+int prepare(tdc_processor *p, const StartOpts &o, int &launches);
+int upload_grid(tdc_processor *p, int &launches);
+int choose_path(const tdc_processor *p);
+void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg);
+int stage_bytes_for(int s_pad, int &cb);
+FocusJob make_job(const tdc_processor *p, float4 *partial, int cb);
+// Plan units (p->units_host) and make sure the processor's scratch holds them and the partials.
+int focus_plan(tdc_processor *p, FocusPlan &plan);
+
+}  // namespace impl
+}  // namespace tdc

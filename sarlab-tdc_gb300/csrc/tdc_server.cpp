@@ -1,0 +1,556 @@
+// tdc_server.cpp -- persistent request loop of the GB300 TDC engine: continuous
+// batching of focus jobs with memory-based admission. No reference counterpart
+// (the reference processes one acquisition per blocking start() call).
+//
+// Jobs are submitted from any host thread and run on one GPU:
+//  * admission: a job enters when a processor slot is free and its device
+//    footprint fits in the memory budget next to the resident jobs (FIFO, so a
+//    large job is not overtaken forever); its acquisition and grid are then
+//    copied and prepared on the slot's own stream while other jobs compute;
+//  * batching: each launch of the focus kernel carries work units (pixel tile x
+//    chirp group) from every active job, the work split evenly between them, so
+//    a job that arrives while others are on the GPU shares the next launch with
+//    them; at most two launches are queued so the GPU never waits for the host;
+//  * completion: after the launch holding a job's last units, its partials are
+//    reduced and the image copied back on the same stream; the host collects it
+//    when the job's event completes.
+// Each job keeps its own decomposition (depending only on its shape) and its
+// own partial buffer reduced in a fixed order, so a job's image is bitwise the
+// same alone and in any mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "tdc_gb300.h"
+#include "tdc_internal.h"
+#include "tdc_processor_impl.h"
+
+using namespace tdc;
+using namespace tdc::impl;
+
+namespace {
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+enum JobState { kQueued = 0, kActive = 1, kCompleting = 2, kDone = 3, kFailed = 4 };
+
+struct Job {
+    uint64_t id = 0;
+    tdc_job_desc d{};
+    std::vector<float> pos32;  // FP32 copy of FP64-only positions (windows / skip test)
+    double t_submit = 0, t_admit = 0, t_first = -1, t_done = 0;
+    tdc_processor *slot = nullptr;
+    FocusPlan plan;
+    size_t next_unit = 0;
+    size_t n_units = 0;
+    double unit_work = 0;  // correlations per unit
+    size_t footprint = 0;
+    int state = kQueued;
+    int rc = TDC_OK;
+    std::string err;
+    cudaEvent_t done_ev = nullptr;
+};
+
+struct Batch {
+    DevBuf dev;        // [counter, status | jobs | units]
+    PinnedBuf host;    // staging of jobs + units, status read-back
+    cudaEvent_t ev = nullptr;
+    bool in_flight = false;
+    std::vector<Job *> finishing;  // jobs whose last units are in this batch
+    std::vector<Job *> members;
+};
+
+constexpr size_t kBatchOffJobs = 256;
+constexpr int kMaxBatchJobs = 64;
+
+size_t device_footprint(const tdc_job_desc &d, int n_sm)
+{
+    const size_t C = (size_t)d.n_pri, S = (size_t)d.n_samples, P = (size_t)d.n_pix;
+    const size_t s_pad = round_up(S, kSampleAlign);
+    int groups = 1, cpg = d.n_pri;
+    plan_groups((long long)P, d.n_pri, std::max(1, n_sm * 3), groups, cpg);
+    const size_t n_tiles = (P + kFocusTile - 1) / kFocusTile;
+    size_t b = 0;
+    b += C * s_pad * 8;                 // samples
+    b += C * sizeof(ChirpRec);          // records
+    b += ((C + kChunk - 1) / kChunk) * 9 * sizeof(SkipPoint);
+    b += S * 8 + S * 4 + C * 24;        // frequency table, range window, base positions
+    b += P * 3 * (d.grid_f64 ? 8 : 4);  // grid staging
+    b += P * 16 * (d.grid_f64 ? 2 : 1); // grid hi / lo
+    b += 1024 + n_tiles * groups * sizeof(FocusUnit) + (size_t)groups * P * 16;  // scratch
+    b += P * 8;                         // image
+    return b;
+}
+
+size_t slot_bytes(const tdc_processor *p)
+{
+    return p->xw.cap + p->chirps.cap + p->skip.cap + p->gs.cap + p->pos_base.cap + p->wr.cap + p->offsets.cap +
+           p->grid_stage.cap + p->grid_hi.cap + p->grid_lo.cap + p->scratch.cap + p->adj_scratch.cap +
+           p->image_dev.cap;
+}
+
+// Give an idle slot's device memory back (cudaFree synchronises the device, so
+// this runs only when an admission would otherwise exceed the budget).
+void release_slot(tdc_processor *p)
+{
+    for (DevBuf *b : {&p->xw, &p->chirps, &p->skip, &p->gs, &p->pos_base, &p->wr, &p->offsets, &p->grid_stage,
+                      &p->grid_hi, &p->grid_lo, &p->scratch, &p->adj_scratch, &p->image_dev})
+        b->release();
+    p->prepared = false;
+    p->plan_path = -1;
+    p->plan_uploaded = false;
+}
+
+}  // namespace
+
+struct tdc_server {
+    int device = 0;
+    int n_sm = 0;
+    size_t budget = 0;
+    int max_jobs = 0;
+    double batch_work = 0;  // correlations per launch (sets the admission / fairness granularity)
+    double t0 = 0;
+
+    std::vector<tdc_processor *> slots;
+    std::vector<tdc_processor *> free_slots;
+    std::deque<Job *> queue;
+    std::vector<Job *> active;
+    std::vector<Job *> completing;
+    std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
+    uint64_t next_id = 1;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    bool stop = false;
+    std::thread th;
+    int thread_rc = TDC_OK;
+    std::string thread_err;
+
+    cudaStream_t compute = nullptr;
+    Batch batches[2];
+    int next_batch = 0;
+    tdc_server_stats stats{};
+
+    void loop();
+    int admit_one(Job *j);
+    void launch_batch();
+    void collect();
+    void fail_job(Job *j, int rc, const std::string &msg);
+};
+
+void tdc_server::fail_job(Job *j, int rc, const std::string &msg)
+{
+    j->rc = rc;
+    j->err = msg;
+    j->state = kFailed;
+    j->t_done = now_ms() - t0;
+    if (j->slot) {
+        free_slots.push_back(j->slot);
+        j->slot = nullptr;
+    }
+    stats.jobs_failed++;
+}
+
+int tdc_server::admit_one(Job *j)
+{
+    tdc_processor *p = j->slot;
+    const tdc_job_desc &d = j->d;
+    int rc = tdc_processor_set_raw_data(p, d.raw_iq, nullptr, d.sample_times, j->pos32.empty() ? d.position : j->pos32.data(),
+                                        d.velocity, d.attitude, d.n_pri, d.n_samples, d.mod_rate, d.start_freq,
+                                        d.body_boresight);
+    if (!rc) rc = tdc_processor_set_trajectory_per_chirp(p, j->pos32.empty() ? d.position : j->pos32.data(),
+                                                         d.velocity, d.attitude);
+    if (!rc && d.position_f64) rc = tdc_processor_set_chirp_positions_f64(p, d.position_f64, d.n_pri);
+    if (!rc) {
+        const int rows = 1;
+        const int cols = (int)d.n_pix;
+        rc = d.grid_f64 ? tdc_processor_set_focus_grid_f64(p, d.grid_f64, rows, cols)
+                        : tdc_processor_set_focus_grid(p, d.grid, rows, cols);
+    }
+    if (!rc) rc = tdc_processor_prepare(p, d.doppler_win_center, d.doppler_bandwidth, d.dop_centroid_win,
+                                        d.apply_range_win, d.doppler_win_taper);
+    if (!rc) rc = tdc_processor_upload_grid(p);
+    if (!rc) rc = focus_plan(p, j->plan);
+    if (rc) return rc;
+    if (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess || p->image_host.ensure((size_t)p->P * 8) != cudaSuccess)
+        return set_last_error(TDC_ERR_NO_MEMORY, "image buffers");
+    j->n_units = p->units_host.size();
+    j->next_unit = 0;
+    j->unit_work = (double)kFocusTile * j->plan.job.chirps_per_group * d.n_samples;
+    return TDC_OK;
+}
+
+void tdc_server::collect()
+{
+    // Launch status words and completed jobs.
+    for (Batch &b : batches) {
+        if (!b.in_flight || cudaEventQuery(b.ev) != cudaSuccess) continue;
+        b.in_flight = false;
+        const int status = reinterpret_cast<int *>(b.host.p)[1];
+        if (status & kStatusTimeout) {
+            for (Job *j : b.members)
+                if (j->state == kActive || j->state == kCompleting) {
+                    j->rc = TDC_ERR_TIMEOUT;
+                    j->err = "focus kernel wait timed out";
+                }
+        }
+    }
+    for (size_t i = 0; i < completing.size();) {
+        Job *j = completing[i];
+        if (cudaEventQuery(j->done_ev) != cudaSuccess) {
+            ++i;
+            continue;
+        }
+        if (j->rc == TDC_OK) {
+            std::memcpy(j->d.image, j->slot->image_host.p, (size_t)j->d.n_pix * 8);
+            j->state = kDone;
+            stats.jobs_done++;
+            stats.correlations += (int64_t)j->d.n_pix * j->d.n_pri * j->d.n_samples;
+        } else {
+            j->state = kFailed;
+            stats.jobs_failed++;
+        }
+        j->t_done = now_ms() - t0;
+        free_slots.push_back(j->slot);
+        j->slot = nullptr;
+        completing.erase(completing.begin() + i);
+        cv_done.notify_all();
+    }
+}
+
+void tdc_server::launch_batch()
+{
+    Batch &b = batches[next_batch];
+    if (b.in_flight) {
+        cudaEventSynchronize(b.ev);
+        collect();
+    }
+    // Jobs of this launch: the active FP32-bulk jobs with units left (oldest first).
+    std::vector<Job *> members;
+    for (Job *j : active)
+        if (j->next_unit < j->n_units && (int)members.size() < kMaxBatchJobs) members.push_back(j);
+    if (members.empty()) return;
+    // Fair share of the launch's work, leftovers to the jobs that can use them.
+    std::vector<size_t> take(members.size(), 0);
+    double left = batch_work;
+    for (int round = 0; round < 4 && left > 0; ++round) {
+        size_t open = 0;
+        for (size_t i = 0; i < members.size(); ++i)
+            if (members[i]->next_unit + take[i] < members[i]->n_units) ++open;
+        if (!open) break;
+        const double share = left / open;
+        for (size_t i = 0; i < members.size(); ++i) {
+            Job *j = members[i];
+            const size_t rem = j->n_units - j->next_unit - take[i];
+            if (!rem) continue;
+            size_t n = (size_t)std::max(1.0, share / j->unit_work);
+            n = std::min(n, rem);
+            take[i] += n;
+            left -= n * j->unit_work;
+        }
+    }
+    size_t n_units = 0;
+    for (size_t t : take) n_units += t;
+    const size_t off_units = round_up(kBatchOffJobs + members.size() * sizeof(FocusJob), 256);
+    const size_t bytes = off_units + n_units * sizeof(FocusUnit);
+    if (b.dev.ensure(bytes) != cudaSuccess || b.host.ensure(bytes) != cudaSuccess) {
+        for (Job *j : members) {
+            j->rc = TDC_ERR_NO_MEMORY;
+            j->err = "batch buffers";
+        }
+        return;
+    }
+    unsigned char *h = static_cast<unsigned char *>(b.host.p);
+    std::memset(h, 0, kBatchOffJobs);
+    FocusJob *hj = reinterpret_cast<FocusJob *>(h + kBatchOffJobs);
+    FocusUnit *hu = reinterpret_cast<FocusUnit *>(h + off_units);
+    int stage_bytes = 0;
+    size_t u = 0;
+    b.finishing.clear();
+    b.members = members;
+    const double t = now_ms() - t0;
+    for (size_t i = 0; i < members.size(); ++i) {
+        Job *j = members[i];
+        hj[i] = j->plan.job;
+        stage_bytes = std::max(stage_bytes, j->plan.stage_bytes);
+        for (size_t k = 0; k < take[i]; ++k) {
+            FocusUnit fu = j->slot->units_host[j->next_unit + k];
+            fu.job = (int)i;
+            hu[u++] = fu;
+        }
+        j->next_unit += take[i];
+        if (j->t_first < 0) j->t_first = t;
+        if (j->next_unit == j->n_units) b.finishing.push_back(j);
+    }
+    int err = 0;
+    err |= cudaMemcpyAsync(b.dev.p, b.host.p, bytes, cudaMemcpyHostToDevice, compute) != cudaSuccess;
+    const int bps = focus_fp32_blocks_per_sm(stage_bytes);
+    const int grid = (int)std::min<size_t>(n_units, (size_t)std::max(1, n_sm * bps));
+    unsigned char *d = static_cast<unsigned char *>(b.dev.p);
+    err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
+                             reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
+                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, compute) != cudaSuccess;
+    err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, compute) != cudaSuccess;
+    stats.launches++;
+    for (Job *j : b.finishing) {
+        tdc_processor *p = j->slot;
+        const long long P = p->P;
+        err |= launch_focus_reduce(j->plan.job.partial, j->plan.job.n_groups, P, p->image_dev.as<float2>(), compute) !=
+               cudaSuccess;
+        err |= cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, compute) !=
+               cudaSuccess;
+        err |= cudaEventRecord(j->done_ev, compute) != cudaSuccess;
+        j->state = kCompleting;
+        completing.push_back(j);
+        active.erase(std::find(active.begin(), active.end(), j));
+    }
+    err |= cudaEventRecord(b.ev, compute) != cudaSuccess;
+    b.in_flight = true;
+    next_batch ^= 1;
+    if (err) {
+        for (Job *j : members) {
+            j->rc = TDC_ERR_CUDA;
+            j->err = "batch launch failed";
+        }
+    }
+}
+
+void tdc_server::loop()
+{
+    cudaSetDevice(device);
+    for (;;) {
+        // 1. admission (outside the lock for the heavy part)
+        Job *cand = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            collect();
+            if (stop && queue.empty() && active.empty() && completing.empty()) break;
+            size_t in_use = 0;
+            for (tdc_processor *p : slots) in_use += slot_bytes(p);
+            if (!queue.empty() && !free_slots.empty()) {
+                Job *j = queue.front();
+                // the free slot that needs the least growth
+                tdc_processor *best = nullptr;
+                size_t best_growth = (size_t)-1;
+                for (tdc_processor *p : free_slots) {
+                    const size_t have = slot_bytes(p);
+                    const size_t growth = j->footprint > have ? j->footprint - have : 0;
+                    if (growth < best_growth) {
+                        best_growth = growth;
+                        best = p;
+                    }
+                }
+                if (j->footprint > budget) {
+                    queue.pop_front();
+                    fail_job(j, TDC_ERR_NO_MEMORY, "job needs more device memory than the server budget");
+                    cv_done.notify_all();
+                    continue;
+                }
+                // Idle slots may hold memory from earlier jobs: release the largest first.
+                while (in_use + best_growth > budget) {
+                    tdc_processor *victim = nullptr;
+                    for (tdc_processor *p : free_slots)
+                        if (p != best && slot_bytes(p) > 0 && (!victim || slot_bytes(p) > slot_bytes(victim)))
+                            victim = p;
+                    if (!victim) break;
+                    in_use -= slot_bytes(victim);
+                    release_slot(victim);
+                }
+                if (in_use + best_growth <= budget || (active.empty() && completing.empty())) {
+                    queue.pop_front();
+                    free_slots.erase(std::find(free_slots.begin(), free_slots.end(), best));
+                    j->slot = best;
+                    cand = j;
+                }
+            }
+            if (!cand && active.empty()) {
+                if (completing.empty()) {
+                    cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                    continue;
+                }
+            }
+        }
+        if (cand) {
+            cand->t_admit = now_ms() - t0;
+            const int rc = admit_one(cand);
+            std::lock_guard<std::mutex> lk(mu);
+            if (rc) {
+                fail_job(cand, rc, tdc_last_error());
+                cv_done.notify_all();
+            } else if (cand->plan.path != TDC_PATH_FP32_BULK) {
+                // FP64 / general path: not batched, focused on its own.
+                tdc_processor *p = cand->slot;
+                const int rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), compute);
+                if (rc2) {
+                    fail_job(cand, rc2, tdc_last_error());
+                } else {
+                    cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
+                                    compute);
+                    cudaEventRecord(cand->done_ev, compute);
+                    cand->t_first = now_ms() - t0;
+                    cand->state = kCompleting;
+                    completing.push_back(cand);
+                }
+            } else {
+                cand->state = kActive;
+                active.push_back(cand);
+            }
+            continue;  // admit as many as fit before the next launch
+        }
+        // 2. keep two launches queued
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (!active.empty()) launch_batch();
+        }
+        // 3. idle wait for the oldest launch or a completion
+        {
+            Batch &b = batches[next_batch];
+            if (b.in_flight) cudaEventSynchronize(b.ev);
+            else if (!completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(200));
+        }
+    }
+}
+
+extern "C" {
+
+int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_server **out)
+{
+    if (!out) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (max_jobs <= 0) max_jobs = 8;
+    if (cudaSetDevice(device) != cudaSuccess) return set_last_error(TDC_ERR_CUDA, "cudaSetDevice failed");
+    auto s = std::make_unique<tdc_server>();
+    s->device = device;
+    s->max_jobs = std::min(max_jobs, kMaxBatchJobs);
+    cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, device);
+    if (memory_budget_bytes == 0) {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        memory_budget_bytes = free_b / 2;
+    }
+    s->budget = memory_budget_bytes;
+    s->batch_work = 2.0e11;  // ~25 ms of work per launch at ~8 Tcorr/s
+    s->t0 = now_ms();
+    if (cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking) != cudaSuccess)
+        return set_last_error(TDC_ERR_CUDA, "stream creation failed");
+    for (Batch &b : s->batches)
+        if (cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming) != cudaSuccess)
+            return set_last_error(TDC_ERR_CUDA, "event creation failed");
+    for (int i = 0; i < s->max_jobs; ++i) {
+        tdc_processor *p = nullptr;
+        if (int rc = tdc_processor_create(device, &p)) return rc;
+        s->slots.push_back(p);
+        s->free_slots.push_back(p);
+    }
+    tdc_server *raw = s.release();
+    raw->th = std::thread([raw] { raw->loop(); });
+    *out = raw;
+    return TDC_OK;
+}
+
+int tdc_server_submit(tdc_server *s, const tdc_job_desc *job, uint64_t *job_id)
+{
+    if (!s || !job || !job_id) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null argument");
+    if (job->n_pri <= 0) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "nPri must be greater than 0");
+    if (job->n_samples <= 0) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "nSamples must be greater than 0");
+    if (job->n_pix <= 0 || job->n_pix > 0x7fffffff)
+        return set_last_error(TDC_ERR_INVALID_ARGUMENT, "n_pix out of range");
+    if (!job->raw_iq || !job->sample_times || !job->image || !(job->position || job->position_f64) ||
+        !(job->grid || job->grid_f64))
+        return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null input array");
+    auto j = std::make_unique<Job>();
+    j->d = *job;
+    if (!job->position) {
+        j->pos32.resize((size_t)job->n_pri * 3);
+        for (size_t i = 0; i < j->pos32.size(); ++i) j->pos32[i] = (float)job->position_f64[i];
+    }
+    j->footprint = device_footprint(*job, s->n_sm);
+    if (cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming) != cudaSuccess)
+        return set_last_error(TDC_ERR_CUDA, "event creation failed");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return set_last_error(TDC_ERR_STATE, "server is shutting down");
+    j->id = s->next_id++;
+    j->t_submit = now_ms() - s->t0;
+    *job_id = j->id;
+    s->queue.push_back(j.get());
+    s->jobs.emplace(j->id, std::move(j));
+    s->stats.jobs_submitted++;
+    s->cv_work.notify_all();
+    return TDC_OK;
+}
+
+int tdc_server_wait(tdc_server *s, uint64_t job_id, int timeout_ms, tdc_job_info *info)
+{
+    if (!s) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end()) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "unknown job id");
+    Job *j = it->second.get();
+    auto done = [j] { return j->state == kDone || j->state == kFailed; };
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, done);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) {
+        return set_last_error(TDC_ERR_TIMEOUT, "job not finished");
+    }
+    if (info) {
+        info->submit_ms = j->t_submit;
+        info->admit_ms = j->t_admit;
+        info->first_launch_ms = j->t_first;
+        info->done_ms = j->t_done;
+        info->correlations = (int64_t)j->d.n_pix * j->d.n_pri * j->d.n_samples;
+        info->status = j->rc;
+        info->path = j->plan.path;
+    }
+    if (j->rc) return set_last_error(j->rc, j->err);
+    return TDC_OK;
+}
+
+int tdc_server_stats_get(tdc_server *s, tdc_server_stats *out)
+{
+    if (!s || !out) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    size_t in_use = 0;
+    for (tdc_processor *p : s->slots) in_use += slot_bytes(p);
+    out->device_bytes_in_use = (int64_t)in_use;
+    out->queued = (int)s->queue.size();
+    out->active = (int)(s->active.size() + s->completing.size());
+    return TDC_OK;
+}
+
+int tdc_server_destroy(tdc_server *s)
+{
+    if (!s) return TDC_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->th.joinable()) s->th.join();
+    cudaSetDevice(s->device);
+    if (s->compute) cudaStreamSynchronize(s->compute);
+    for (auto &kv : s->jobs)
+        if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
+    for (Batch &b : s->batches)
+        if (b.ev) cudaEventDestroy(b.ev);
+    for (tdc_processor *p : s->slots) tdc_processor_destroy(p);
+    if (s->compute) cudaStreamDestroy(s->compute);
+    delete s;
+    return TDC_OK;
+}
+
+}  // extern "C"

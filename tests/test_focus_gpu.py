@@ -255,3 +255,19 @@ def test_cpp_tdcprocessor_smoke(cuda_device, tmp_path):
 
     r = subprocess.run([str(_cpp_build(tmp_path))], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_per_chirp_trajectory_matches_per_sample_arrays(cuda_device):
+    """setTrajectoryPerChirp (ingest extension) gives the same image as the reference's per-sample arrays."""
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=81, n_pri=300, n_samples=80, nx=20, ny=18, device="cuda")
+    api = _moving_api(sc, speed=0.03)
+    args = (1.0, 25.0, True, True, True)
+    img, _, _ = run_engine(api, sc.grid, args)
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setTrajectoryPerChirp(api["position"][:, 0, :], api["velocity"][:, 0, :], api["attitude"][:, 0, :])
+    p.setFocusGrid(sc.grid)
+    p.start(*args)
+    np.testing.assert_array_equal(p.getFocusedImage(), img)

@@ -1,0 +1,108 @@
+"""GPU tests of the request loop: results identical alone and in a mix,
+memory-based admission, overlap of a job arriving while another runs, and
+rejection of a job larger than the budget."""
+import time
+
+import numpy as np
+import pytest
+
+from sarlabtdc import scenes
+
+pytestmark = pytest.mark.gpu
+
+START = (0.0, float("inf"), False, False, True)
+
+
+def _jobs():
+    shapes = [  # (nx, ny, n_pri, n_samples, seed)
+        (64, 48, 384, 256, 1), (100, 37, 160, 128, 2), (32, 32, 900, 64, 3),
+        (128, 128, 256, 512, 4), (17, 5, 1024, 32, 5), (96, 80, 512, 96, 6),
+    ]
+    out = []
+    for nx, ny, C, S, seed in shapes:
+        sc = scenes.small_scene(seed=seed, n_pri=C, n_samples=S, nx=nx, ny=ny, jitter=0.2e-3, device="cuda")
+        out.append(sc)
+    return out
+
+
+def _submit(srv, sc, f64=True):
+    return srv.submit(sc.raw, sc.radar.sample_times(), sc.positions if f64 else sc.positions.astype(np.float32),
+                      sc.grid if f64 else sc.grid.astype(np.float32), np.float32(sc.radar.mod_rate),
+                      np.float32(sc.radar.f0), start=START)
+
+
+def test_same_result_alone_and_in_mix_and_as_processor(cuda_device):
+    import _sarlabtdc
+    from sarlabtdc.serving import FocusServer
+
+    jobs = _jobs()
+    with FocusServer(max_jobs=4) as srv:
+        alone = []
+        for sc in jobs:
+            img, info = srv.wait(_submit(srv, sc))
+            assert info["status"] == 0
+            alone.append(img)
+        ids = [_submit(srv, sc) for sc in jobs]          # all at once: they share launches
+        mixed = [srv.wait(i)[0] for i in ids]
+        st = srv.stats()
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(a, m)
+    assert st["jobs_done"] == 2 * len(jobs)
+    # and the same as the processor (tdc_processor_focus_device path)
+    for sc, a in zip(jobs, alone):
+        p = _sarlabtdc.TdcProcessor(0)
+        api = sc.api_arrays()
+        p.setRawData(*api.values())
+        p.setChirpPositionsF64(sc.positions)
+        p.setFocusGridF64(sc.grid)
+        p.start(*START)
+        np.testing.assert_array_equal(p.getFocusedImage().ravel(), a)
+
+
+def test_admission_under_a_tight_budget(cuda_device):
+    from sarlabtdc.serving import FocusServer
+
+    jobs = _jobs()
+    budget = 96 << 20
+    with FocusServer(memory_budget=budget, max_jobs=6) as srv:
+        ids = [_submit(srv, sc) for sc in jobs]
+        peak = 0
+        while True:
+            st = srv.stats()
+            peak = max(peak, st["device_bytes_in_use"])
+            if st["jobs_done"] + st["jobs_failed"] == len(jobs):
+                break
+            time.sleep(0.002)
+        for i in ids:
+            img, info = srv.wait(i)
+            assert info["status"] == 0 and np.isfinite(img).all()
+    assert peak <= budget
+
+
+def test_job_arriving_during_a_long_job_overlaps_it(cuda_device):
+    from sarlabtdc.serving import FocusServer
+
+    long = scenes.small_scene(seed=9, n_pri=4096, n_samples=512, nx=768, ny=768, device="cuda")
+    short = scenes.small_scene(seed=10, n_pri=256, n_samples=128, nx=32, ny=32, device="cuda")
+    with FocusServer(max_jobs=4) as srv:
+        lid = _submit(srv, long)
+        time.sleep(0.05)
+        sid = _submit(srv, short)
+        _, si = srv.wait(sid)
+        _, li = srv.wait(lid)
+    assert si["first_launch_ms"] < li["done_ms"]      # started while the long job was on the GPU
+    assert si["done_ms"] < li["done_ms"]              # and finished before it
+
+
+def test_job_over_budget_fails_alone(cuda_device):
+    from sarlabtdc.serving import FocusServer
+
+    big = scenes.small_scene(seed=11, n_pri=512, n_samples=512, nx=256, ny=256, device="cuda")
+    small = scenes.small_scene(seed=12, n_pri=128, n_samples=64, nx=16, ny=16, device="cuda")
+    with FocusServer(memory_budget=8 << 20, max_jobs=2) as srv:
+        bid = _submit(srv, big)
+        sid = _submit(srv, small)
+        with pytest.raises(MemoryError):
+            srv.wait(bid)
+        img, info = srv.wait(sid)
+        assert info["status"] == 0
