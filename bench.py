@@ -49,8 +49,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="2", choices=["1", "2", "3"],
-                    help="1: 256^2 stripmap, 1024 x 512; 2: precision study (default); 3: 3-D volume")
+    ap.add_argument("--config", default="2", choices=["1", "2", "3", "4", "5"],
+                    help="1: 256^2 stripmap, 1024 x 512; 2: precision study (default); 3: 3-D volume; "
+                         "4: serving mix; 5: autofocus")
+    ap.add_argument("--jobs", type=int, default=256, help="config 4: number of requests")
+    ap.add_argument("--rate", type=float, default=20.0, help="config 4: mean arrivals per second")
+    ap.add_argument("--af-steps", type=int, default=50, help="config 5: Adam steps")
+    ap.add_argument("--af-lr", type=float, default=5e-5, help="config 5: Adam learning rate [m]")
     ap.add_argument("--side", type=int, default=1024, help="grid side (pixels), config 2")
     ap.add_argument("--chirps", type=int, default=4096, help="config 2")
     ap.add_argument("--samples", type=int, default=1024, help="config 2")
@@ -413,6 +418,180 @@ def run_ours(args):
     print(json.dumps(out), flush=True)
 
 
+def run_serving(args):
+    """Config 4: a seeded Poisson stream of focus requests through the request loop, against
+    the same jobs run one after another through the processor (FIFO, same arrival times)."""
+    import threading
+
+    from sarlabtdc import scenes
+    from sarlabtdc.serving import FocusServer
+
+    rng = np.random.default_rng(4)
+    n = args.jobs
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    sides = rng.choice([128, 256, 512, 1024, 2048], n)
+    chirps = np.round(np.exp(rng.uniform(np.log(256), np.log(8192), n))).astype(int)
+    samples = rng.choice([256, 512, 1024], n)
+    ntg = rng.integers(1, 101, n)
+    t = time.time()
+    jobs = []
+    for i in range(n):
+        radar = scenes.Radar(n_samples=int(samples[i]))
+        pos = scenes.rail(int(chirps[i]), int(chirps[i]) * 0.25e-3, 0.3)
+        side = int(sides[i])
+        grid = scenes.ground_grid(side, side, 1.0 / side, y0=0.3).astype(np.float32)
+        lo, hi = grid.reshape(-1, 3).min(0), grid.reshape(-1, 3).max(0)
+        tg = np.zeros((int(ntg[i]), 3))
+        tg[:, 0] = rng.uniform(lo[0], hi[0], tg.shape[0])
+        tg[:, 1] = rng.uniform(lo[1], hi[1], tg.shape[0])
+        amps = np.exp(2j * np.pi * rng.uniform(0, 1, tg.shape[0]))
+        raw = scenes.simulate_raw(pos, tg, amps, radar, "cuda").astype(np.complex64)
+        jobs.append(dict(raw=raw, st=radar.sample_times(), pos=pos.astype(np.float32), grid=grid,
+                         K=np.float32(radar.mod_rate), f0=np.float32(radar.f0),
+                         corr=side * side * int(chirps[i]) * int(samples[i])))
+    log(f"serving: generated {n} jobs in {time.time() - t:.0f}s; "
+        f"{sum(j['corr'] for j in jobs) / 1e12:.1f} Tcorr total")
+    start = (0.0, float("inf"), False, False, True)
+
+    # request loop
+    with FocusServer(max_jobs=16) as srv:
+        ids = [None] * n
+        t0 = time.perf_counter()
+
+        def client():
+            for i, j in enumerate(jobs):
+                dt = arrivals[i] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                ids[i] = srv.submit(j["raw"], j["st"], j["pos"], j["grid"], j["K"], j["f0"], start=start)
+
+        th = threading.Thread(target=client)
+        th.start()
+        th.join()
+        infos = [srv.wait(i)[1] for i in ids]
+        st = srv.stats()
+    lat = np.array([x["done_ms"] - x["submit_ms"] for x in infos])
+    span = max(x["done_ms"] for x in infos) - min(x["submit_ms"] for x in infos)
+    total = sum(j["corr"] for j in jobs)
+    served = {"p50_ms": round(float(np.percentile(lat, 50)), 1), "p99_ms": round(float(np.percentile(lat, 99)), 1),
+              "gcorr_s": round(total / (span / 1e3) / 1e9, 1), "span_s": round(span / 1e3, 2),
+              "launches": st["launches"]}
+    log(f"request loop: {served}")
+
+    # serial: the same jobs one at a time (each alone on the GPU), FIFO on the same arrivals
+    service = []
+    with FocusServer(max_jobs=1) as one:
+        for j in jobs:
+            t = time.perf_counter()
+            one.wait(one.submit(j["raw"], j["st"], j["pos"], j["grid"], j["K"], j["f0"], start=start))
+            service.append(time.perf_counter() - t)
+    finish, lat_s = 0.0, []
+    for a, sv in zip(arrivals, service):
+        finish = max(finish, a) + sv
+        lat_s.append(finish - a)
+    lat_s = np.array(lat_s) * 1e3
+    serial = {"p50_ms": round(float(np.percentile(lat_s, 50)), 1), "p99_ms": round(float(np.percentile(lat_s, 99)), 1),
+              "gcorr_s": round(total / (finish - arrivals[0]) / 1e9, 1), "span_s": round(finish - arrivals[0], 2)}
+    log(f"serial: {serial}")
+    out = {"metric": "serving: p50/p99 focus latency and aggregate Gcorr/s", "value": served["gcorr_s"],
+           "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic (seeded Poisson arrivals, point targets)",
+           "config": {"workload": f"serving mix: {n} requests, Poisson {args.rate}/s, grids 128^2..2048^2, "
+                                  "256..8192 chirps (log-uniform), 256/512/1024 samples, 1-100 targets",
+                      "total_correlations": total},
+           "latency_ms": {"p50": served["p50_ms"], "p99": served["p99_ms"]},
+           "request_loop": served, "serial_processor": serial,
+           "offered_gcorr_s": round(total / (arrivals[-1] - arrivals[0]) / 1e9, 1)}
+    print(json.dumps(out), flush=True)
+
+
+def run_autofocus(args):
+    """Config 5: entropy autofocus of a random-walk trajectory error through the adjoint kernel."""
+    import torch
+
+    import _sarlabtdc
+    import oracle
+    from sarlabtdc import autofocus, scenes
+
+    sc = scenes.config5(device="cuda")
+    api = sc.api_arrays()
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setChirpPositionsF64(sc.positions)
+    p.setFocusGridF64(sc.grid)
+    op = autofocus.FocusOperator(p, (0.0, float("inf"), False, False, True))
+    corr = sc.correlations()
+    # timing of forward and adjoint
+    zero = torch.zeros((sc.n_pri, 3), dtype=torch.float64, device="cuda")
+    g = torch.randn(op.n_pix, dtype=torch.complex64, device="cuda")
+    op.image(zero)
+    op.adjoint(zero, g)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    img = op.image(zero)
+    e[1].record()
+    op.adjoint(zero, g)
+    e[2].record()
+    torch.cuda.synchronize()
+    fwd_ms, adj_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    # gradient check on a pixel subset: engine adjoint vs FP64 oracle and vs FD of the engine
+    rng = np.random.default_rng(55)
+    pix = rng.choice(op.n_pix, 96, replace=False)
+    gsub = np.zeros(op.n_pix, np.complex64)
+    gsub[pix] = (rng.normal(size=pix.size) + 1j * rng.normal(size=pix.size)).astype(np.complex64)
+    off = rng.normal(0, 0.05e-3, (sc.n_pri, 3))
+    got = op.adjoint(torch.from_numpy(off).cuda(), torch.from_numpy(gsub).cuda()).cpu().numpy()
+    build_oracle()
+    prob = oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions,
+                          modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid)
+    ref = oracle.adjoint_offsets(prob, oracle_opts(), off, gsub[pix].astype(np.complex128), pixels=pix)
+    grad_err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    h = 1e-6
+    fd_rel = []
+    offt = torch.from_numpy(off).cuda()
+    for c, k in [(100, 0), (2000, 1), (3500, 2)]:
+        ep = np.array(off)
+        em = np.array(off)
+        ep[c, k] += h
+        em[c, k] -= h
+        lp = float(np.real(np.sum(np.conj(gsub[pix]) * oracle.focus(
+            oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions + ep,
+                           modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid), oracle_opts(),
+            pixels=pix))))
+        lm = float(np.real(np.sum(np.conj(gsub[pix]) * oracle.focus(
+            oracle.Problem(raw=api["rawData"], sampleTimes=api["sampleTimes"], position=sc.positions + em,
+                           modRate=api["modRate"], startFreq=api["startFreq"], grid=sc.grid), oracle_opts(),
+            pixels=pix))))
+        fd = (lp - lm) / (2 * h)
+        fd_rel.append(abs(got[c, k] - fd) / max(abs(fd), 1e-30))
+    # autofocus
+    walk = sc.meta["walk"]
+    centre = sc.grid.reshape(-1, 3).mean(0)
+    lam = float(oracle.wavelength_center(api["sampleTimes"], api["modRate"], api["startFreq"]))
+    ph0 = autofocus.residual_phase_rms(np.zeros_like(walk), walk, sc.positions, centre, lam)
+    ideal = op.image(torch.from_numpy(walk).cuda()).cpu().numpy()
+    coh0 = autofocus.coherence(op.image(None).cpu().numpy(), ideal)
+    res = autofocus.autofocus(op, steps=args.af_steps, lr=args.af_lr)
+    ph1 = autofocus.residual_phase_rms(res.offsets.cpu().numpy(), walk, sc.positions, centre, lam)
+    coh1 = autofocus.coherence(op.image(res.offsets).cpu().numpy(), ideal)
+    out = {"metric": "autofocus: adjoint accuracy, entropy, residual phase, time per Adam step",
+           "value": round(float(np.mean(res.step_ms)), 2), "unit": "ms/Adam step", "higher_is_better": False,
+           "n_gpus": 1, "dtype": "f32",
+           "data": "synthetic (seeded random-walk trajectory error, 30 targets)",
+           "config": {"workload": "autofocus: 512x512 px @1mm, 4096 chirps x 1024 samples over 2 m, random walk "
+                                  "0.2 mm/step", "correlations_per_forward": corr},
+           "forward_ms": round(fwd_ms, 2), "adjoint_ms": round(adj_ms, 2),
+           "forward_gcorr_s": round(corr / (fwd_ms / 1e3) / 1e9, 1),
+           "adjoint_gcorr_s": round(corr / (adj_ms / 1e3) / 1e9, 1),
+           "gradient_vs_fp64_oracle_rel_l2": grad_err, "gradient_vs_central_fd_h1e-6_rel": fd_rel,
+           "entropy": {"start": res.entropy[0], "end": res.entropy[-1]},
+           "residual_phase_rms_rad": {"start": ph0, "end": ph1},
+           "coherence_with_true_trajectory_image": {"start": coh0, "end": coh1},
+           "adam_steps": args.af_steps, "lr_m": args.af_lr}
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return
@@ -465,6 +644,10 @@ def main():
         return 2
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "4":
+        run_serving(args)
+    elif args.config == "5":
+        run_autofocus(args)
     else:
         run_ours(args)
     return 0

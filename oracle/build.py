@@ -2,6 +2,11 @@
 
 * ``oracle/_build/libtdc_oracle.so`` -- the FP64 C restatement in
   ``oracle/tdc_oracle.c`` (gcc -O2 -fopenmp).
+* ``oracle/_ref/tdckernels.ptx`` -- the reference's own GPU kernels
+  (``tdc-lib/src/tdckernels.cu``) compiled to PTX by nvcc from where the source
+  lies in the reference checkout (fmt from torch's bundled headers). PTX is
+  architecture-neutral text, so it travels to the GPU machine, where
+  tests/golden/make_ref_gpu_golden.py runs those kernels to record golden images.
 * ``oracle/_ref/libtdc_refmath.so`` -- the reference's own host-side math
   (``tdc-lib/include/gpumath.h`` and ``windowing.h``, compiled from where they
   lie in the reference checkout by g++, through ``oracle/ref_math_shim.cpp``).
@@ -72,10 +77,41 @@ def build_refmath(force: bool = False) -> Path | None:
     return REFMATH_SO
 
 
+REF_PTX = REF_OUT / "tdckernels.ptx"
+
+
+def build_ref_ptx(force: bool = False) -> Path | None:
+    """PTX of the reference's tdckernels.cu (built only where the checkout is present)."""
+    root = reference_root()
+    if root is None:
+        return REF_PTX if REF_PTX.exists() else None
+    src = root / "tdc-lib" / "src" / "tdckernels.cu"
+    inc = root / "tdc-lib" / "include"
+    if not force and not _stale(REF_PTX, [src, inc / "gpumath.h", inc / "windowing.h", inc / "tuning.h",
+                                          Path(__file__)]):
+        return REF_PTX
+    try:
+        import torch.utils.cpp_extension as ext
+        torch_inc = ext.include_paths()[0]
+    except Exception:
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    tmp = REF_PTX.with_suffix(".ptx.tmp%d" % os.getpid())
+    cmd = [nvcc, "-ptx", "-arch=compute_103a", "-std=c++17", "-DFMT_HEADER_ONLY", "-I", str(inc), "-I", torch_inc,
+           "-w", str(src), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    os.replace(tmp, REF_PTX)
+    return REF_PTX
+
+
 def main(argv: list[str]) -> int:
     force = "--force" in argv
     print(build_oracle(force))
     print(build_refmath(force))
+    print(build_ref_ptx(force))
     return 0
 
 

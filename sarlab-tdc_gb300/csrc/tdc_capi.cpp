@@ -423,7 +423,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb)
     return job;
 }
 
-int focus_plan(tdc_processor *p, FocusPlan &plan)
+int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 {
     if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
     if (p->P <= 0) return fail(TDC_ERR_STATE, "no focus grid");
@@ -442,8 +442,18 @@ int focus_plan(tdc_processor *p, FocusPlan &plan)
         slots = p->n_sm * 4;
     }
 
-    if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots) {
+    if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
+        max_unit_work != p->plan_unit_cap) {
         plan_groups(P, C, slots, p->plan_groups, p->plan_cpg);
+        if (max_unit_work > 0) {
+            // bound the work of one unit (tile x chirp group): at most cap / (tile x S) chirps per group
+            const int cpg_cap = std::max(1, (int)(max_unit_work / ((double)kFocusTile * p->S)));
+            if (p->plan_cpg > cpg_cap) {
+                p->plan_cpg = cpg_cap;
+                p->plan_groups = (C + cpg_cap - 1) / cpg_cap;
+            }
+        }
+        p->plan_unit_cap = max_unit_work;
         const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
         p->units_host.clear();
         p->units_host.reserve((size_t)(n_tiles * p->plan_groups));

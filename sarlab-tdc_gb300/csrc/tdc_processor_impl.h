@@ -149,6 +149,7 @@ struct tdc_processor {
     std::vector<tdc::FocusUnit> units_host;
     long long plan_P = -1;
     int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0;
+    double plan_unit_cap = 0.0;
     bool plan_uploaded = false;
 
     // Adjoint (autofocus) scratch.
@@ -182,7 +183,8 @@ void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg);
 int stage_bytes_for(int s_pad, int &cb);
 FocusJob make_job(const tdc_processor *p, float4 *partial, int cb);
 // Plan units (p->units_host) and make sure the processor's scratch holds them and the partials.
-int focus_plan(tdc_processor *p, FocusPlan &plan);
+// max_unit_work > 0 bounds the correlations of one unit (the request loop's granularity).
+int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work = 0.0);
 
 }  // namespace impl
 }  // namespace tdc

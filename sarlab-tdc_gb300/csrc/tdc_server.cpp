@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -77,12 +78,19 @@ struct Batch {
 constexpr size_t kBatchOffJobs = 256;
 constexpr int kMaxBatchJobs = 64;
 
+// Correlations per work unit in the request loop: one launch of ~1e12 correlations
+// (~130 ms) holds at least two units per resident CTA.
+constexpr double kServerUnitWork = 1.0e9;
+constexpr double kServerBatchWork = 1.0e12;
+
 size_t device_footprint(const tdc_job_desc &d, int n_sm)
 {
     const size_t C = (size_t)d.n_pri, S = (size_t)d.n_samples, P = (size_t)d.n_pix;
     const size_t s_pad = round_up(S, kSampleAlign);
     int groups = 1, cpg = d.n_pri;
     plan_groups((long long)P, d.n_pri, std::max(1, n_sm * 3), groups, cpg);
+    const int cpg_cap = std::max(1, (int)(kServerUnitWork / ((double)kFocusTile * S)));
+    if (cpg > cpg_cap) groups = (d.n_pri + cpg_cap - 1) / cpg_cap;
     const size_t n_tiles = (P + kFocusTile - 1) / kFocusTile;
     size_t b = 0;
     b += C * s_pad * 8;                 // samples
@@ -184,7 +192,7 @@ int tdc_server::admit_one(Job *j)
     if (!rc) rc = tdc_processor_prepare(p, d.doppler_win_center, d.doppler_bandwidth, d.dop_centroid_win,
                                         d.apply_range_win, d.doppler_win_taper);
     if (!rc) rc = tdc_processor_upload_grid(p);
-    if (!rc) rc = focus_plan(p, j->plan);
+    if (!rc) rc = focus_plan(p, j->plan, kServerUnitWork);
     if (rc) return rc;
     if (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess || p->image_host.ensure((size_t)p->P * 8) != cudaSuccess)
         return set_last_error(TDC_ERR_NO_MEMORY, "image buffers");
@@ -239,29 +247,31 @@ void tdc_server::launch_batch()
         cudaEventSynchronize(b.ev);
         collect();
     }
-    // Jobs of this launch: the active FP32-bulk jobs with units left (oldest first).
+    // Jobs of this launch, oldest first: each takes what is left of the launch's work
+    // budget (first come, first served), and later jobs backfill the rest, so a job
+    // that arrives while others run shares their launches. A launch holds at least
+    // two units per resident CTA so the GPU stays full.
     std::vector<Job *> members;
     for (Job *j : active)
         if (j->next_unit < j->n_units && (int)members.size() < kMaxBatchJobs) members.push_back(j);
     if (members.empty()) return;
-    // Fair share of the launch's work, leftovers to the jobs that can use them.
+    const size_t min_units = (size_t)std::max(1, 2 * n_sm * 3);
     std::vector<size_t> take(members.size(), 0);
     double left = batch_work;
-    for (int round = 0; round < 4 && left > 0; ++round) {
-        size_t open = 0;
-        for (size_t i = 0; i < members.size(); ++i)
-            if (members[i]->next_unit + take[i] < members[i]->n_units) ++open;
-        if (!open) break;
-        const double share = left / open;
-        for (size_t i = 0; i < members.size(); ++i) {
-            Job *j = members[i];
-            const size_t rem = j->n_units - j->next_unit - take[i];
-            if (!rem) continue;
-            size_t n = (size_t)std::max(1.0, share / j->unit_work);
-            n = std::min(n, rem);
-            take[i] += n;
-            left -= n * j->unit_work;
-        }
+    size_t taken = 0;
+    for (size_t i = 0; i < members.size() && (left > 0 || taken < min_units); ++i) {
+        Job *j = members[i];
+        const size_t rem = j->n_units - j->next_unit;
+        size_t n = (size_t)std::ceil(std::max(0.0, left) / j->unit_work);
+        n = std::max(n, min_units > taken ? min_units - taken : (size_t)0);
+        n = std::min(std::max<size_t>(n, 1), rem);
+        take[i] = n;
+        taken += n;
+        left -= n * j->unit_work;
+    }
+    while (!members.empty() && take.back() == 0) {
+        members.pop_back();
+        take.pop_back();
     }
     size_t n_units = 0;
     for (size_t t : take) n_units += t;
@@ -443,7 +453,7 @@ int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_
         memory_budget_bytes = free_b / 2;
     }
     s->budget = memory_budget_bytes;
-    s->batch_work = 2.0e11;  // ~25 ms of work per launch at ~8 Tcorr/s
+    s->batch_work = kServerBatchWork;
     s->t0 = now_ms();
     if (cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking) != cudaSuccess)
         return set_last_error(TDC_ERR_CUDA, "stream creation failed");

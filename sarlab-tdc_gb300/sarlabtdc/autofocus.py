@@ -106,6 +106,13 @@ def autofocus(op: FocusOperator, steps: int = 50, lr: float = 2e-5, offsets: tor
     return res
 
 
+def coherence(a, b) -> float:
+    """|<a, b>| / (|a| |b|): 1 when two images agree up to a common complex factor."""
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    return float(np.abs(np.vdot(a, b)) / (np.linalg.norm(a) * np.linalg.norm(b)))
+
+
 def residual_phase_rms(offsets_est: np.ndarray, offsets_true: np.ndarray, positions: np.ndarray,
                        centre: np.ndarray, wavelength: float) -> float:
     """RMS over chirps of the two-way phase error 4 pi / lambda * u_c . (true - estimate) towards the scene
