@@ -212,10 +212,10 @@ int tdc_processor_adjoint_device(tdc_processor *proc, const float *grad_image_de
 /*
  * A persistent request loop on one GPU: jobs submitted from any host thread are
  * admitted while a processor slot is free and their device footprint fits in
- * the memory budget next to the resident jobs (first come, first admitted);
- * every focus launch carries work units of all admitted jobs (continuous
- * batching, work split evenly between them). A job's image is bitwise the same
- * whether it ran alone or in a mix.
+ * the memory budget next to the resident jobs; each focus launch carries work
+ * units of the admitted jobs (continuous batching), filled in priority order:
+ * least estimated remaining service time, aged by the time waited so no job
+ * starves. A job's image is bitwise the same whether it ran alone or in a mix.
  */
 typedef struct tdc_server tdc_server;
 
@@ -263,7 +263,7 @@ typedef struct tdc_server_stats {
     int active;
 } tdc_server_stats;
 
-/* memory_budget_bytes = 0: half of the free device memory; max_jobs = 0: 8. */
+/* memory_budget_bytes = 0: half of the free device memory; max_jobs = 0: 32 (at most 64). */
 int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_server **out);
 /* Inputs are borrowed until the job is done. */
 int tdc_server_submit(tdc_server *srv, const tdc_job_desc *job, uint64_t *job_id);

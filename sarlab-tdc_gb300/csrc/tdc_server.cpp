@@ -3,14 +3,17 @@
 // (the reference processes one acquisition per blocking start() call).
 //
 // Jobs are submitted from any host thread and run on one GPU:
-//  * admission: a job enters when a processor slot is free and its device
-//    footprint fits in the memory budget next to the resident jobs (FIFO, so a
-//    large job is not overtaken forever); its acquisition and grid are then
-//    copied and prepared on the slot's own stream while other jobs compute;
+//  * priority: least estimated remaining service time first, aged by the time
+//    a job has waited (so short jobs finish fast and long ones are not starved);
+//  * admission: the highest-priority queued job enters when a processor slot is
+//    free and its device footprint fits in the memory budget next to the
+//    resident jobs; its acquisition and grid are copied and prepared on the
+//    slot's own stream while other jobs compute;
 //  * batching: each launch of the focus kernel carries work units (pixel tile x
-//    chirp group) from every active job, the work split evenly between them, so
-//    a job that arrives while others are on the GPU shares the next launch with
-//    them; at most two launches are queued so the GPU never waits for the host;
+//    chirp group, bounded in size) of the active jobs in priority order, later
+//    jobs backfilling what the first leave free, so a job that arrives while
+//    others are on the GPU joins the next launch; at most two launches are
+//    queued so the GPU never waits for the host;
 //  * completion: after the launch holding a job's last units, its partials are
 //    reduced and the image copied back on the same stream; the host collects it
 //    when the job's event completes.
@@ -82,6 +85,10 @@ constexpr int kMaxBatchJobs = 64;
 // (~130 ms) holds at least two units per resident CTA.
 constexpr double kServerUnitWork = 1.0e9;
 constexpr double kServerBatchWork = 1.0e12;
+// Priority: shortest estimated remaining service first, aged so that waiting jobs
+// are not starved (a job gains kAging seconds of priority per second it waits).
+constexpr double kRateEstimate = 7.0e12;  // correlations per second
+constexpr double kAging = 0.5;
 
 size_t device_footprint(const tdc_job_desc &d, int n_sm)
 {
@@ -152,6 +159,15 @@ struct tdc_server {
     Batch batches[2];
     int next_batch = 0;
     tdc_server_stats stats{};
+
+    // Scheduling priority (lower first): estimated remaining service time minus
+    // kAging x time waited since submission, in seconds.
+    double score(const Job *j, double t_ms) const
+    {
+        const double rem = j->state == kQueued ? (double)j->d.n_pix * j->d.n_pri * j->d.n_samples
+                                               : (double)(j->n_units - j->next_unit) * j->unit_work;
+        return rem / kRateEstimate - kAging * (t_ms - j->t_submit) / 1e3;
+    }
 
     void loop();
     int admit_one(Job *j);
@@ -247,14 +263,21 @@ void tdc_server::launch_batch()
         cudaEventSynchronize(b.ev);
         collect();
     }
-    // Jobs of this launch, oldest first: each takes what is left of the launch's work
-    // budget (first come, first served), and later jobs backfill the rest, so a job
-    // that arrives while others run shares their launches. A launch holds at least
-    // two units per resident CTA so the GPU stays full.
+    // Jobs of this launch in priority order (least remaining service time, aged by the
+    // wait): each takes what is left of the launch's work budget and the next ones
+    // backfill the rest, so a job that arrives while others run joins the next launch
+    // and short jobs finish first. A launch holds at least two units per resident CTA
+    // so the GPU stays full.
     std::vector<Job *> members;
     for (Job *j : active)
-        if (j->next_unit < j->n_units && (int)members.size() < kMaxBatchJobs) members.push_back(j);
+        if (j->next_unit < j->n_units) members.push_back(j);
     if (members.empty()) return;
+    {
+        const double t = now_ms() - t0;
+        std::stable_sort(members.begin(), members.end(),
+                         [&](Job *a, Job *b) { return score(a, t) < score(b, t); });
+        if ((int)members.size() > kMaxBatchJobs) members.resize(kMaxBatchJobs);
+    }
     const size_t min_units = (size_t)std::max(1, 2 * n_sm * 3);
     std::vector<size_t> take(members.size(), 0);
     double left = batch_work;
@@ -352,7 +375,17 @@ void tdc_server::loop()
             size_t in_use = 0;
             for (tdc_processor *p : slots) in_use += slot_bytes(p);
             if (!queue.empty() && !free_slots.empty()) {
-                Job *j = queue.front();
+                // Queued job with the least estimated remaining service time, aged by its wait.
+                const double t = now_ms() - t0;
+                Job *j = nullptr;
+                for (Job *q : queue)
+                    if (!j || score(q, t) < score(j, t)) j = q;
+                if (j->footprint > budget) {
+                    queue.erase(std::find(queue.begin(), queue.end(), j));
+                    fail_job(j, TDC_ERR_NO_MEMORY, "job needs more device memory than the server budget");
+                    cv_done.notify_all();
+                    continue;
+                }
                 // the free slot that needs the least growth
                 tdc_processor *best = nullptr;
                 size_t best_growth = (size_t)-1;
@@ -363,12 +396,6 @@ void tdc_server::loop()
                         best_growth = growth;
                         best = p;
                     }
-                }
-                if (j->footprint > budget) {
-                    queue.pop_front();
-                    fail_job(j, TDC_ERR_NO_MEMORY, "job needs more device memory than the server budget");
-                    cv_done.notify_all();
-                    continue;
                 }
                 // Idle slots may hold memory from earlier jobs: release the largest first.
                 while (in_use + best_growth > budget) {
@@ -381,7 +408,7 @@ void tdc_server::loop()
                     release_slot(victim);
                 }
                 if (in_use + best_growth <= budget || (active.empty() && completing.empty())) {
-                    queue.pop_front();
+                    queue.erase(std::find(queue.begin(), queue.end(), j));
                     free_slots.erase(std::find(free_slots.begin(), free_slots.end(), best));
                     j->slot = best;
                     cand = j;
@@ -441,7 +468,7 @@ int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_
 {
     if (!out) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null output pointer");
     *out = nullptr;
-    if (max_jobs <= 0) max_jobs = 8;
+    if (max_jobs <= 0) max_jobs = 32;
     if (cudaSetDevice(device) != cudaSuccess) return set_last_error(TDC_ERR_CUDA, "cudaSetDevice failed");
     auto s = std::make_unique<tdc_server>();
     s->device = device;

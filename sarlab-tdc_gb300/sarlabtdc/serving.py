@@ -17,7 +17,7 @@ import _tdc_capi as _lib
 
 
 class FocusServer:
-    def __init__(self, device: int = 0, memory_budget: int = 0, max_jobs: int = 8):
+    def __init__(self, device: int = 0, memory_budget: int = 0, max_jobs: int = 32):
         h = C.c_void_p()
         _lib.check(_lib.lib().tdc_server_create(int(device), int(memory_budget), int(max_jobs), C.byref(h)))
         self._h = h

@@ -82,7 +82,7 @@ def test_admission_under_a_tight_budget(cuda_device):
 def test_job_arriving_during_a_long_job_overlaps_it(cuda_device):
     from sarlabtdc.serving import FocusServer
 
-    long = scenes.small_scene(seed=9, n_pri=4096, n_samples=512, nx=768, ny=768, device="cuda")
+    long = scenes.small_scene(seed=9, n_pri=4096, n_samples=512, nx=1536, ny=1536, device="cuda")
     short = scenes.small_scene(seed=10, n_pri=256, n_samples=128, nx=32, ny=32, device="cuda")
     with FocusServer(max_jobs=4) as srv:
         lid = _submit(srv, long)
