@@ -188,6 +188,12 @@ int tdc_processor_num_pixels(const tdc_processor *proc, int64_t *n_pix);
 /* tdc_path the next focus will take, or -1 when nothing is resident. */
 int tdc_processor_path(const tdc_processor *proc);
 
+/* 1 when the processor's kernels read the caller's host arrays in place (the
+ * device reports coherent access to pageable host memory, as over Grace-Blackwell
+ * NVLink-C2C; TDC_GB300_HOST_READS=0 in the environment turns it off at
+ * creation), 0 when inputs are staged by copies. */
+int tdc_processor_reads_host_memory(const tdc_processor *proc);
+
 /* ---- autofocus (no reference counterpart) ---- */
 
 /* Antenna positions of the resident acquisition := base + offsets_dev[c] (device,

@@ -188,6 +188,10 @@ class TdcProcessor:
         _lib.check(_lib.lib().tdc_processor_num_pixels(self._h, C.byref(n)))
         return n.value
 
+    def readsHostMemory(self) -> bool:
+        """True when the kernels read the input arrays in place over a coherent host link."""
+        return bool(_lib.lib().tdc_processor_reads_host_memory(self._h))
+
     def path(self) -> str:
         return _lib.PATH_NAMES.get(_lib.lib().tdc_processor_path(self._h), "none")
 

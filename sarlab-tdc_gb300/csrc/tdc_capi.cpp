@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -157,8 +158,25 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     // Trajectory element of (chirp c, sample s): per-sample arrays, or one row per chirp.
     const bool tpc = p->traj_per_chirp;
     auto ti = [tpc, S](long c, long s) -> size_t { return tpc ? (size_t)c : (size_t)c * S + s; };
-    p->per_chirp = tpc || ((p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
-                           rows_constant(p->att, C, S, 4));
+    if (tpc) {
+        p->per_chirp = true;
+    } else if (p->host_reads) {
+        // The device reads the caller's per-sample arrays in place (coherent host access)
+        // and reports whether any chirp's samples differ.
+        TDC_CK(p->flag.ensure(16), "alloc flag");
+        TDC_CK(cudaMemsetAsync(p->flag.p, 0, 4, p->stream), "reset flag");
+        if (!p->pos64) TDC_CK(launch_rows_differ(p->pos, C, S, 3, p->flag.as<int>(), p->stream), "scan kernel");
+        if (p->vel) TDC_CK(launch_rows_differ(p->vel, C, S, 3, p->flag.as<int>(), p->stream), "scan kernel");
+        if (p->att) TDC_CK(launch_rows_differ(p->att, C, S, 4, p->flag.as<int>(), p->stream), "scan kernel");
+        int differ = 0;
+        TDC_CK(cudaMemcpyAsync(&differ, p->flag.p, 4, cudaMemcpyDeviceToHost, p->stream), "read flag");
+        TDC_CK(cudaStreamSynchronize(p->stream), "scan sync");
+        p->per_chirp = differ == 0;
+        launches += (!p->pos64) + (p->vel != nullptr) + (p->att != nullptr);
+    } else {
+        p->per_chirp = (p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
+                       rows_constant(p->att, C, S, 4);
+    }
     fit_frequencies(p->sample_times, S, p->start_freq, p->mod_rate, p->F0, p->F1, p->resid_hz);
     for (int k = 0; k < 3; ++k) {
         p->ant_min[k] = std::numeric_limits<double>::infinity();
@@ -267,9 +285,11 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(p->gs.ensure((size_t)S * 8), "alloc frequency table");
     TDC_CK(p->pos_base.ensure((size_t)C * 3 * 8), "alloc base positions");
 
-    TDC_CK(cudaMemcpy2DAsync(p->xw.p, (size_t)s_pad * 8, p->raw, (size_t)S * 8, (size_t)S * 8, C,
-                             cudaMemcpyHostToDevice, st),
-           "copy raw data");
+    if (!p->host_reads) {
+        TDC_CK(cudaMemcpy2DAsync(p->xw.p, (size_t)s_pad * 8, p->raw, (size_t)S * 8, (size_t)S * 8, C,
+                                 cudaMemcpyHostToDevice, st),
+               "copy raw data");
+    }
     TDC_CK(cudaMemcpyAsync(p->chirps.p, recs.data(), n_rec * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
            "copy chirp records");
     TDC_CK(cudaMemcpyAsync(p->skip.p, skip.data(), skip.size() * sizeof(SkipPoint), cudaMemcpyHostToDevice, st),
@@ -282,7 +302,14 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
 
     TDC_CK(launch_range_window(p->wr.as<float>(), S, o.range_win, st), "range window kernel");
-    TDC_CK(launch_prewindow(p->xw.as<float2>(), p->wr.as<float>(), C, S, s_pad, st), "prewindow kernel");
+    if (p->host_reads) {
+        // Window and pad straight from the caller's buffer (read over the coherent host link).
+        TDC_CK(launch_prewindow_from(reinterpret_cast<const float2 *>(p->raw), p->wr.as<float>(), C, S, s_pad,
+                                     p->xw.as<float2>(), st),
+               "prewindow kernel");
+    } else {
+        TDC_CK(launch_prewindow(p->xw.as<float2>(), p->wr.as<float>(), C, S, s_pad, st), "prewindow kernel");
+    }
     launches += 2;
     // The host vectors above are read by the async copies: wait before they go out of scope.
     TDC_CK(cudaStreamSynchronize(st), "prepare sync");
@@ -299,35 +326,56 @@ int upload_grid(tdc_processor *p, int &launches)
     if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
     const long long P = (long long)p->rows * p->cols;
     p->P = P;
-    for (int k = 0; k < 3; ++k) {
-        p->grid_min[k] = std::numeric_limits<double>::infinity();
-        p->grid_max[k] = -std::numeric_limits<double>::infinity();
-    }
-    for (long long i = 0; i < P; ++i)
-        for (int k = 0; k < 3; ++k) {
-            const double v = p->grid64 ? p->grid64[3 * i + k] : (double)p->grid[3 * i + k];
-            p->grid_min[k] = std::min(p->grid_min[k], v);
-            p->grid_max[k] = std::max(p->grid_max[k], v);
-        }
     cudaStream_t st = p->stream;
     const size_t elt = p->grid64 ? 8 : 4;
-    TDC_CK(p->grid_stage.ensure((size_t)P * 3 * elt), "alloc grid staging");
     TDC_CK(p->grid_hi.ensure((size_t)P * 16), "alloc grid");
-    TDC_CK(cudaMemcpyAsync(p->grid_stage.p, p->grid64 ? (const void *)p->grid64 : (const void *)p->grid,
-                           (size_t)P * 3 * elt, cudaMemcpyHostToDevice, st),
-           "copy grid");
+    const void *src = p->grid64 ? (const void *)p->grid64 : (const void *)p->grid;
+    if (!p->host_reads) {
+        for (int k = 0; k < 3; ++k) {
+            p->grid_min[k] = std::numeric_limits<double>::infinity();
+            p->grid_max[k] = -std::numeric_limits<double>::infinity();
+        }
+        for (long long i = 0; i < P; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const double v = p->grid64 ? p->grid64[3 * i + k] : (double)p->grid[3 * i + k];
+                p->grid_min[k] = std::min(p->grid_min[k], v);
+                p->grid_max[k] = std::max(p->grid_max[k], v);
+            }
+        TDC_CK(p->grid_stage.ensure((size_t)P * 3 * elt), "alloc grid staging");
+        TDC_CK(cudaMemcpyAsync(p->grid_stage.p, src, (size_t)P * 3 * elt, cudaMemcpyHostToDevice, st), "copy grid");
+        src = p->grid_stage.p;
+    }
     p->stats.h2d_bytes += (int64_t)P * 3 * elt;
     if (p->grid64) {
         TDC_CK(p->grid_lo.ensure((size_t)P * 16), "alloc grid");
-        TDC_CK(launch_grid_from_f64(p->grid_stage.as<double>(), P, p->grid_hi.as<float4>(),
+        TDC_CK(launch_grid_from_f64(static_cast<const double *>(src), P, p->grid_hi.as<float4>(),
                                     p->grid_lo.as<float4>(), st),
                "grid kernel");
         p->grid_lo_valid = true;
     } else {
-        TDC_CK(launch_grid_from_f32(p->grid_stage.as<float>(), P, p->grid_hi.as<float4>(), st), "grid kernel");
+        TDC_CK(launch_grid_from_f32(static_cast<const float *>(src), P, p->grid_hi.as<float4>(), st), "grid kernel");
         p->grid_lo_valid = false;
     }
     launches += 1;
+    if (p->host_reads && P > 0) {
+        // bounding box of the grid on the device (order-preserving integer keys of the floats)
+        const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000,
+                             (int)0x80000000};
+        int keys[6];
+        TDC_CK(p->flag.ensure(64), "alloc flag");
+        int *box = p->flag.as<int>() + 4;
+        TDC_CK(cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st), "init bbox");
+        TDC_CK(launch_grid_bbox(p->grid_hi.as<float4>(), P, box, st), "bbox kernel");
+        TDC_CK(cudaMemcpyAsync(keys, box, sizeof(keys), cudaMemcpyDeviceToHost, st), "read bbox");
+        TDC_CK(cudaStreamSynchronize(st), "grid sync");
+        launches += 1;
+        for (int k = 0; k < 6; ++k) {
+            const int bits = keys[k] >= 0 ? keys[k] : keys[k] ^ 0x7fffffff;
+            float f;
+            std::memcpy(&f, &bits, 4);
+            (k < 3 ? p->grid_min[k] : p->grid_max[k - 3]) = f;
+        }
+    }
     return TDC_OK;
 }
 
@@ -564,6 +612,14 @@ int tdc_processor_create(int gpu_num, tdc_processor **out)
     if (!p) return fail(TDC_ERR_NO_MEMORY, "out of host memory");
     p->device = gpu_num;
     e = cudaDeviceGetAttribute(&p->n_sm, cudaDevAttrMultiProcessorCount, gpu_num);
+    if (e == cudaSuccess) {
+        // Coherent access to pageable host memory (Grace-Blackwell NVLink-C2C): the
+        // kernels then read the caller's arrays in place instead of staging copies.
+        int pageable = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, gpu_num);
+        const char *env = std::getenv("TDC_GB300_HOST_READS");
+        p->host_reads = pageable == 1 && !(env && env[0] == '0');
+    }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&p->ev[i]);
     if (e != cudaSuccess) {
@@ -814,6 +870,11 @@ int tdc_processor_num_pixels(const tdc_processor *p, int64_t *n)
     if (int rc = check_proc(p)) return rc;
     if (n) *n = p->P;
     return TDC_OK;
+}
+
+int tdc_processor_reads_host_memory(const tdc_processor *p)
+{
+    return p && p->host_reads ? 1 : 0;
 }
 
 int tdc_processor_path(const tdc_processor *p)

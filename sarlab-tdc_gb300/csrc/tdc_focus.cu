@@ -39,11 +39,7 @@ namespace {
 #ifndef TDC_FOCUS_MINB
 #define TDC_FOCUS_MINB 3
 #endif
-// Paired-FP32 (FFMA2) inner loop: samples are expanded in shared memory to
-// (xr, xr, xi, -xi) so one __ffma2_rn does two of the four FMAs of a complex MAC.
-#ifndef TDC_FOCUS_FFMA2
-#define TDC_FOCUS_FFMA2 0
-#endif
+
 constexpr int kL = TDC_FOCUS_L;  // in-block phasor table length
 
 struct SharedPixel {
@@ -85,9 +81,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     __shared__ FocusJob sJ;
 
     SharedPixel &sp = *reinterpret_cast<SharedPixel *>(smem + kFocusStages * stage_bytes);
-#if TDC_FOCUS_FFMA2
-    float4 *xdup = reinterpret_cast<float4 *>(smem + kFocusStages * stage_bytes + sizeof(SharedPixel));
-#endif
+
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -190,17 +184,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
             const ChirpRec *recs = reinterpret_cast<const ChirpRec *>(base + CB * row_bytes);
             const int cb0 = c0 + j * CB;
             const int cnt = min(CB, c1 - cb0);
-#if TDC_FOCUS_FFMA2
-            {
-                const float2 *xn = reinterpret_cast<const float2 *>(base);
-                const int n = cnt * s_pad;
-                for (int e = tid; e < n; e += kFocusThreads) {
-                    const float2 v = xn[e];
-                    xdup[e] = make_float4(v.x, v.x, v.y, -v.y);
-                }
-                __syncthreads();
-            }
-#endif
 
             for (int cc = 0; cc < cnt; ++cc) {
                 const int c = cb0 + cc;
@@ -256,45 +239,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     h[i] = make_float2(0.f, 0.f);
                 }
 
-#if TDC_FOCUS_FFMA2
-                // Split accumulators: A = (xr pr, xr pi) terms, B = (xi pr, -xi pi) terms;
-                // H = (A.x + B.y, A.y + B.x). Horner step: A = (hr, hr) (qr, qi), B = (hi, hi) (qr, -qi).
-                {
-                    (void)xs;
-                    const float4 *xd = xdup + (size_t)cc * s_pad;
-                    const float2 one0 = make_float2(1.0f, 0.0f);
-                    float2 A[kFocusPT], B[kFocusPT], qa[kFocusPT], qb[kFocusPT];
-#pragma unroll
-                    for (int i = 0; i < kFocusPT; ++i) {
-                        A[i] = make_float2(0.f, 0.f);
-                        B[i] = make_float2(0.f, 0.f);
-                        qa[i] = ql[i];
-                        qb[i] = make_float2(ql[i].x, -ql[i].y);
-                    }
-#pragma unroll 2
-                    for (int b = nb - 1; b >= 0; --b) {
-#pragma unroll
-                        for (int i = 0; i < kFocusPT; ++i) {
-                            const float hr = A[i].x + B[i].y, hi = A[i].y + B[i].x;
-                            A[i] = __fmul2_rn(make_float2(hr, hr), qa[i]);
-                            B[i] = __fmul2_rn(make_float2(hi, hi), qb[i]);
-                        }
-#pragma unroll
-                        for (int k = 0; k < kL; ++k) {
-                            const float4 x = xd[b * kL + k];
-                            const float2 xrr = make_float2(x.x, x.y), xin = make_float2(x.z, x.w);
-#pragma unroll
-                            for (int i = 0; i < kFocusPT; ++i) {
-                                const float2 pk = k == 0 ? one0 : p[i][k > 0 ? k - 1 : 0];
-                                A[i] = __ffma2_rn(xrr, pk, A[i]);
-                                B[i] = __ffma2_rn(xin, pk, B[i]);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int i = 0; i < kFocusPT; ++i) h[i] = make_float2(A[i].x + B[i].y, A[i].y + B[i].x);
-                }
-#else
                 // Horner over blocks, last block first.
 #pragma unroll 2
                 for (int b = nb - 1; b >= 0; --b) {
@@ -304,7 +248,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
 #pragma unroll
                     for (int i = 0; i < kFocusPT; ++i) h[i] = horner_block(h[i], ql[i], p[i], xv);
                 }
-#endif
 
 #pragma unroll
                 for (int i = 0; i < kFocusPT; ++i) {
@@ -377,12 +320,7 @@ __global__ void focus_reduce_kernel(const float4 *__restrict__ partial, int n_gr
 
 int focus_fp32_smem_bytes(int stage_bytes)
 {
-#if TDC_FOCUS_FFMA2
-    // expanded copy of one stage's samples: twice the stage's sample bytes at most
-    return kFocusStages * stage_bytes + (int)sizeof(SharedPixel) + 2 * stage_bytes;
-#else
     return kFocusStages * stage_bytes + (int)sizeof(SharedPixel);
-#endif
 }
 
 int focus_fp32_blocks_per_sm(int stage_bytes)

@@ -97,6 +97,11 @@ enum StatusBits : int {
 cudaError_t launch_range_window(float *w, int n, int apply, cudaStream_t st);
 cudaError_t launch_prewindow(float2 *xw, const float *w, int C, int S, int s_pad, cudaStream_t st);
 cudaError_t launch_chirp_positions(ChirpRec *recs, const double *base, const double *off, int C, cudaStream_t st);
+// Direct-read ingest (source may be pageable host memory where the device reads it coherently).
+cudaError_t launch_prewindow_from(const float2 *src, const float *w, int C, int S, int s_pad, float2 *xw,
+                                  cudaStream_t st);
+cudaError_t launch_rows_differ(const float *a, int C, int S, int k, int *flag, cudaStream_t st);
+cudaError_t launch_grid_bbox(const float4 *hi, long long P, int *out, cudaStream_t st);
 cudaError_t launch_grid_from_f32(const float *grid, long long P, float4 *hi, cudaStream_t st);
 cudaError_t launch_grid_from_f64(const double *grid, long long P, float4 *hi, float4 *lo, cudaStream_t st);
 

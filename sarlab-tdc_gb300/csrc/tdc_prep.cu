@@ -37,6 +37,73 @@ __global__ void prewindow_kernel(float2 *__restrict__ xw, const float *__restric
     }
 }
 
+// Range-windowed, zero-padded rows from a source the device can read directly
+// (device memory, or pageable host memory on a system with coherent host access).
+__global__ void prewindow_from_kernel(const float2 *__restrict__ src, const float *__restrict__ w, int C, int S,
+                                      int s_pad, float2 *__restrict__ xw)
+{
+    const long long total = (long long)C * s_pad;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long c = idx / s_pad;
+        const int s = (int)(idx - c * s_pad);
+        float2 v = make_float2(0.f, 0.f);
+        if (s < S) {
+            const float2 x = src[c * S + s];
+            const float ws = w[s];
+            v = make_float2(x.x * ws, x.y * ws);
+        }
+        xw[idx] = v;
+    }
+}
+
+// flag |= 1 when any sample of a chirp differs (bitwise) from the chirp's first sample;
+// a is [C][S][k] floats.
+__global__ void rows_differ_kernel(const unsigned int *__restrict__ a, int C, int S, int k, int *__restrict__ flag)
+{
+    const long long per = (long long)S * k;
+    const long long total = (long long)C * per;
+    bool differ = false;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long c = idx / per;
+        const long long r = idx - c * per;
+        differ |= a[idx] != a[c * per + (r % k)];
+    }
+    if (__syncthreads_or(differ) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+// Bounding box of the grid's high floats: out = (min x, min y, min z, max x, max y, max z),
+// each as an order-preserving int (see float_key); out must start at (INT_MAX x3, INT_MIN x3).
+__device__ __forceinline__ int float_key(float f)
+{
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+
+__global__ void grid_bbox_kernel(const float4 *__restrict__ hi, long long P, int *__restrict__ out)
+{
+    int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, mx[3] = {(int)0x80000000, (int)0x80000000, (int)0x80000000};
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+        const float4 v = hi[p];
+        const int k[3] = {float_key(v.x), float_key(v.y), float_key(v.z)};
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = min(mn[d], k[d]);
+            mx[d] = max(mx[d], k[d]);
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        for (int off = 16; off > 0; off >>= 1) {
+            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], off));
+            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], off));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&out[d], mn[d]);
+            atomicMax(&out[3 + d], mx[d]);
+        }
+    }
+}
+
 __global__ void grid_f32_kernel(const float *__restrict__ g, long long P, float4 *__restrict__ hi)
 {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -94,6 +161,36 @@ cudaError_t launch_prewindow(float2 *xw, const float *w, int C, int S, int s_pad
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 32) blocks = 152 * 32;
     prewindow_kernel<<<(unsigned)blocks, 256, 0, st>>>(xw, w, C, S, s_pad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prewindow_from(const float2 *src, const float *w, int C, int S, int s_pad, float2 *xw,
+                                  cudaStream_t st)
+{
+    const long long total = (long long)C * s_pad;
+    if (total <= 0) return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    prewindow_from_kernel<<<(unsigned)blocks, 256, 0, st>>>(src, w, C, S, s_pad, xw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rows_differ(const float *a, int C, int S, int k, int *flag, cudaStream_t st)
+{
+    const long long total = (long long)C * S * k;
+    if (total <= 0) return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    rows_differ_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const unsigned int *>(a), C, S, k, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_bbox(const float4 *hi, long long P, int *out, cudaStream_t st)
+{
+    if (P <= 0) return cudaSuccess;
+    long long blocks = (P + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    grid_bbox_kernel<<<(unsigned)blocks, 256, 0, st>>>(hi, P, out);
     return cudaGetLastError();
 }
 

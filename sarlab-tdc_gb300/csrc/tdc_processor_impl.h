@@ -104,6 +104,7 @@ int cuda_fail(cudaError_t e, const char *what);
 struct tdc_processor {
     int device = 0;
     int n_sm = 0;
+    bool host_reads = false;  // the device reads pageable host memory coherently (Grace-Blackwell C2C)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6] = {};
     // Borrowed inputs (setRawData / setFocusGrid).
@@ -136,7 +137,7 @@ struct tdc_processor {
     double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
     double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
     int s_pad = 0, n_chunks = 0;
-    tdc::impl::DevBuf xw, chirps, skip, gs, pos_base, wr, offsets;
+    tdc::impl::DevBuf xw, chirps, skip, gs, pos_base, wr, offsets, flag;
 
     // Device grid.
     long long P = 0;

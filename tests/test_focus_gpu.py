@@ -271,3 +271,29 @@ def test_per_chirp_trajectory_matches_per_sample_arrays(cuda_device):
     p.setFocusGrid(sc.grid)
     p.start(*args)
     np.testing.assert_array_equal(p.getFocusedImage(), img)
+
+
+def test_in_place_host_reads_match_staged_copies(cuda_device, monkeypatch):
+    """Where the device reads pageable host memory coherently, the raw rows, trajectory scan
+    and grid are read in place; the image must equal the staged-copy path bit for bit."""
+    sc = scenes.small_scene(seed=91, n_pri=260, n_samples=72, nx=21, ny=19, jitter=0.1e-3, device="cuda")
+    api = _moving_api(sc, speed=0.02)
+    args = (0.0, 30.0, True, True, True)
+    monkeypatch.setenv("TDC_GB300_HOST_READS", "0")
+    staged, st_a, pa = run_engine(api, sc.grid, args)
+    assert not pa.readsHostMemory()
+    monkeypatch.delenv("TDC_GB300_HOST_READS")
+    direct, st_b, pb = run_engine(api, sc.grid, args, pos64=sc.positions, grid64=None)
+    print("device reads host memory in place:", pb.readsHostMemory())
+    monkeypatch.setenv("TDC_GB300_HOST_READS", "0")
+    staged64, _, _ = run_engine(api, sc.grid, args, pos64=sc.positions)
+    monkeypatch.delenv("TDC_GB300_HOST_READS")
+    direct32, _, _ = run_engine(api, sc.grid, args)
+    np.testing.assert_array_equal(direct32, staged)
+    np.testing.assert_array_equal(direct, staged64)
+    # per-sample motion is detected the same way on both paths
+    pos = api["position"].astype(np.float64)
+    pos[..., 0] += (np.arange(sc.n_samples) / sc.n_samples * 0.2e-3)[None, :]
+    api["position"] = pos.astype(np.float32)
+    _, st_c, _ = run_engine(api, sc.grid, args)
+    assert st_c["path_name"] == "general"
