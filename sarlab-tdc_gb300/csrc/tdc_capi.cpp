@@ -150,6 +150,7 @@ void stats_reset(tdc_processor *p) { std::memset(&p->stats, 0, sizeof(p->stats))
 // Upload + prepare the acquisition for the given start() options.
 int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 {
+    NvtxRange nvtx("tdc prepare");
     if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called before start()");
     const int C = p->C, S = p->S;
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
@@ -323,6 +324,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 // Device grid from a host (FP32 or FP64) grid.
 int upload_grid(tdc_processor *p, int &launches)
 {
+    NvtxRange nvtx("tdc upload grid");
     if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
     const long long P = (long long)p->rows * p->cols;
     p->P = P;
@@ -533,6 +535,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 // Focus the resident acquisition onto the resident grid: image_dev (complex float [P]).
 int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &launches)
 {
+    NvtxRange nvtx("tdc focus");
     FocusPlan plan;
     if (int rc = focus_plan(p, plan)) return rc;
     const long long P = p->P;
@@ -750,6 +753,7 @@ int tdc_processor_start(tdc_processor *p, float doppler_win_center, float dopple
     if (int rc = check_proc(p)) return rc;
     if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called before start()");
     if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
+    NvtxRange nvtx("tdc start");
     const auto t0 = std::chrono::steady_clock::now();
     stats_reset(p);
     int launches = 0;

@@ -9,11 +9,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "tdc_gb300.h"
 #include "tdc_internal.h"
 
 namespace tdc {
 namespace impl {
+
+// NVTX range for profilers (no cost when no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Grow-only device buffer.
 struct DevBuf {

@@ -191,6 +191,7 @@ void tdc_server::fail_job(Job *j, int rc, const std::string &msg)
 
 int tdc_server::admit_one(Job *j)
 {
+    NvtxRange nvtx("tdc server admit");
     tdc_processor *p = j->slot;
     const tdc_job_desc &d = j->d;
     int rc = tdc_processor_set_raw_data(p, d.raw_iq, nullptr, d.sample_times, j->pos32.empty() ? d.position : j->pos32.data(),
@@ -258,6 +259,7 @@ void tdc_server::collect()
 
 void tdc_server::launch_batch()
 {
+    NvtxRange nvtx("tdc server launch");
     Batch &b = batches[next_batch];
     if (b.in_flight) {
         cudaEventSynchronize(b.ev);
