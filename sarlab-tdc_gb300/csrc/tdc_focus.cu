@@ -39,8 +39,15 @@ namespace {
 #ifndef TDC_FOCUS_MINB
 #define TDC_FOCUS_MINB 3
 #endif
+#ifndef TDC_FOCUS_UNROLL
+#define TDC_FOCUS_UNROLL 2
+#endif
+#ifndef TDC_FOCUS_SWAP
+#define TDC_FOCUS_SWAP 0
+#endif
 
 constexpr int kL = TDC_FOCUS_L;  // in-block phasor table length
+constexpr int kUnrollBlocks = TDC_FOCUS_UNROLL;
 
 struct SharedPixel {
     float t[kFocusPT * 6][kFocusThreads];  // (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo) per pixel slot
@@ -63,10 +70,17 @@ __device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2
     for (int k = 1; k < kL; ++k) {
         const float xr = (k & 1) ? xv[k >> 1].z : xv[k >> 1].x;
         const float xi = (k & 1) ? xv[k >> 1].w : xv[k >> 1].y;
+#if TDC_FOCUS_SWAP
+        tr = fmaf(p[k - 1].x, xr, tr);
+        ti = fmaf(p[k - 1].y, xr, ti);
+        tr = fmaf(p[k - 1].y, -xi, tr);
+        ti = fmaf(p[k - 1].x, xi, ti);
+#else
         tr = fmaf(xr, p[k - 1].x, tr);
         tr = fmaf(-xi, p[k - 1].y, tr);
         ti = fmaf(xr, p[k - 1].y, ti);
         ti = fmaf(xi, p[k - 1].x, ti);
+#endif
     }
     return make_float2(tr, ti);
 }
@@ -240,7 +254,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 }
 
                 // Horner over blocks, last block first.
-#pragma unroll 2
+#pragma unroll kUnrollBlocks
                 for (int b = nb - 1; b >= 0; --b) {
                     float4 xv[kL / 2];
 #pragma unroll
