@@ -45,9 +45,9 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps if d.exists())
 
 
-def _compile(src: str) -> tuple[Path, str]:
-    obj = BUILD / (src + ".o")
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
+def _compile(src: str, out_dir: Path, defines: tuple[str, ...]) -> tuple[Path, str]:
+    obj = out_dir / (src + ".o")
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC), *defines]
     if src.endswith(".cu"):
         cmd = [nvcc(), *ARCH, "-lineinfo", "-Xptxas", "-v", *common, "-c", str(CSRC / src), "-o", str(obj)]
     else:
@@ -58,25 +58,28 @@ def _compile(src: str) -> tuple[Path, str]:
     return obj, r.stderr
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
+def build(force: bool = False, verbose: bool = False, defines: tuple[str, ...] = (), out_dir: Path = BUILD,
+          lib: Path = LIB) -> Path:
+    """Compile and link the engine. ``defines`` (``-DNAME=VALUE`` flags) select compile-time
+    variants of the kernels, built into ``out_dir`` / ``lib`` (the focus-kernel tuning sweep)."""
     deps = _deps()
-    if not force and not _stale(LIB, deps):
-        return LIB
-    BUILD.mkdir(exist_ok=True)
+    if not force and not defines and not _stale(lib, deps):
+        return lib
+    out_dir.mkdir(parents=True, exist_ok=True)
     srcs = CU_SOURCES + CPP_SOURCES
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 1)) as ex:
-        results = list(ex.map(_compile, srcs))
-    (BUILD / "ptxas.log").write_text("".join(log for _, log in results))
+        results = list(ex.map(lambda s: _compile(s, out_dir, tuple(defines)), srcs))
+    (out_dir / "ptxas.log").write_text("".join(log for _, log in results))
     objs = [str(o) for o, _ in results]
-    tmp = LIB.with_name(LIB.name + ".tmp%d" % os.getpid())
+    tmp = lib.with_name(lib.name + ".tmp%d" % os.getpid())
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print((BUILD / "ptxas.log").read_text())
-    return LIB
+        print((out_dir / "ptxas.log").read_text())
+    return lib
 
 
 if __name__ == "__main__":

@@ -40,7 +40,7 @@ namespace {
 #define TDC_FOCUS_MINB 3
 #endif
 #ifndef TDC_FOCUS_UNROLL
-#define TDC_FOCUS_UNROLL 2
+#define TDC_FOCUS_UNROLL 8
 #endif
 #ifndef TDC_FOCUS_SWAP
 #define TDC_FOCUS_SWAP 0

@@ -1,0 +1,95 @@
+"""Compile-time tuning sweep of the FP32-bulk focus kernel.
+
+Each variant is the engine rebuilt with extra ``-D`` flags (the kernel's knobs:
+TDC_FOCUS_L, TDC_FOCUS_PT, TDC_FOCUS_MINB, TDC_FOCUS_UNROLL, TDC_FOCUS_SWAP,
+TDC_FOCUS_STAGE_TARGET) into ``_build/variants/<name>/``, then timed on three
+synthetic shapes with the acquisition and grid resident on the device:
+
+    2: 1024^2 pixels x 4096 chirps x 1024 samples (the precision-study size)
+    3: 1024^2 pixels x 4096 chirps x  256 samples (the 3-D volume's sample count)
+    1: 256^2 pixels x 1024 chirps x 512 samples (the small stripmap case)
+
+Timing: 2 warm-up focuses, then the mean of 3 focuses between CUDA events on the
+launching stream. Each variant's image is compared with the first variant's.
+
+    python sarlab-tdc_gb300/tune_focus.py base= u4=-DTDC_FOCUS_UNROLL=4 "s4=-DTDC_FOCUS_SWAP=1 -DTDC_FOCUS_UNROLL=4"
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+SHAPES = ("2", "3", "1")
+
+
+def _time_shape(shape: str, ref_dir: Path) -> dict:
+    sys.path.insert(0, str(PKG))
+    import numpy as np
+    import torch
+
+    import _sarlabtdc
+    from sarlabtdc import scenes
+
+    if shape == "1":
+        sc = scenes.config1(device="cuda")
+    else:
+        sc = scenes.config2(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=1024 if shape == "2" else 256,
+                            n_targets=8)
+    api = sc.api_arrays()
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setChirpPositionsF64(sc.positions)
+    p.setFocusGridF64(sc.grid)
+    p.prepare(0.0, float("inf"), False, False, True)
+    p.uploadGrid()
+    img = torch.empty(p.numPixels(), dtype=torch.complex64, device="cuda")
+    for _ in range(2):
+        p.focusDevice(img)
+    p.check()
+    n = 3
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    for _ in range(n):
+        p.focusDevice(img)
+    ev[1].record()
+    torch.cuda.synchronize()
+    p.check()
+    ms = ev[0].elapsed_time(ev[1]) / n
+    out = img.cpu().numpy()
+    ref_f = ref_dir / f"shape_{shape}.npy"
+    if not ref_f.exists():
+        np.save(ref_f, out)
+    ref = np.load(ref_f)
+    return {"ms": round(ms, 3), "gcorr_s": round(sc.correlations() / (ms / 1e3) / 1e9, 1),
+            "rel_vs_first": float(np.linalg.norm(out - ref) / np.linalg.norm(ref))}
+
+
+def main(argv: list[str]) -> int:
+    if argv[:1] == ["--time"]:
+        print(json.dumps(_time_shape(argv[1], Path(argv[2]))), flush=True)
+        return 0
+    sys.path.insert(0, str(PKG))
+    import build as engine_build
+
+    variants = [a.split("=", 1) for a in argv] or [["base", ""]]
+    ref_dir = Path(tempfile.mkdtemp(prefix="tdc_tune_"))
+    for name, flags in variants:
+        out_dir = engine_build.BUILD / "variants" / name
+        lib = engine_build.build(defines=tuple(flags.split()), out_dir=out_dir, lib=out_dir / "libtdc_gb300.so")
+        for shape in SHAPES:
+            r = subprocess.run([sys.executable, __file__, "--time", shape, str(ref_dir)],
+                               env={**os.environ, "TDC_GB300_LIB": str(lib)}, capture_output=True, text=True,
+                               timeout=900)
+            line = r.stdout.strip().splitlines()[-1] if r.returncode == 0 and r.stdout.strip() else \
+                "failed: " + r.stderr[-400:]
+            print(name, shape, line, flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
