@@ -194,6 +194,17 @@ int tdc_processor_path(const tdc_processor *proc);
  * creation), 0 when inputs are staged by copies. */
 int tdc_processor_reads_host_memory(const tdc_processor *proc);
 
+/* Caller-owned image output (replaces the copy of tdcprocessor_wrapper.cpp:155-163):
+ * later start() calls write the image, n_pix complex floats (interleaved), into
+ * image_host instead of the processor's own buffer, and imageBuffer() returns
+ * image_host. The buffer is borrowed until it is replaced or the processor is
+ * destroyed. Where the device accesses pageable host memory coherently
+ * (tdc_processor_reads_host_memory() = 1) the final reduction kernel writes it
+ * in place, with no device-to-host copy; otherwise the image is copied into it.
+ * n_floats must be >= 2 x the pixels of the grid at start(); image_host = NULL
+ * returns to the processor's own buffer. */
+int tdc_processor_set_image_output(tdc_processor *proc, float *image_host, int64_t n_floats);
+
 /* ---- autofocus (no reference counterpart) ---- */
 
 /* Antenna positions of the resident acquisition := base + offsets_dev[c] (device,

@@ -91,6 +91,11 @@ public:
     }
 
     // ---- extensions (no reference counterpart) ----
+    // Caller-owned image output (nFloats >= 2 x pixels); later start() calls write into it.
+    void setImageOutput(float2 *image, int64_t nFloats)
+    {
+        check(tdc_processor_set_image_output(h_, reinterpret_cast<float *>(image), nFloats));
+    }
     void setChirpPositionsF64(double const *position, int nPri)
     {
         check(tdc_processor_set_chirp_positions_f64(h_, position, nPri));

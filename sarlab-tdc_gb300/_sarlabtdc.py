@@ -25,6 +25,12 @@ def _arr(x, dtype):
     return np.ascontiguousarray(np.asarray(x).astype(dtype, copy=False))
 
 
+def _check_image_array(out, rows, cols):
+    if not isinstance(out, np.ndarray) or out.dtype != np.complex64 or out.shape != (rows, cols) \
+            or not out.flags.c_contiguous or not out.flags.writeable:
+        raise ValueError(f"out must be a writeable C-contiguous complex64 array of shape ({rows}, {cols})")
+
+
 class TdcProcessor:
     """Time-domain correlation SAR processor (tdc-lib/include/tdcprocessor.h:42-200)."""
 
@@ -38,6 +44,7 @@ class TdcProcessor:
         self._pos64_ref = None
         self._grid_rows = 0
         self._grid_cols = 0
+        self._image_out = None
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -112,13 +119,20 @@ class TdcProcessor:
         self._grid_rows, self._grid_cols = rows, cols
         _lib.check(_lib.lib().tdc_processor_set_focus_grid(self._h, _lib.ptr(grid), int(rows), int(cols)))
 
-    def getFocusedImage(self):
-        """tdcprocessor_wrapper.cpp:155-163: a new complex64 [rows, cols] copy of the image."""
+    def getFocusedImage(self, out=None):
+        """tdcprocessor_wrapper.cpp:155-163: a new complex64 [rows, cols] copy of the image.
+
+        Extension: ``out`` (a C-contiguous complex64 [rows, cols] array) receives the copy
+        instead of a new array; the array given to setImageOutput is returned as it is."""
         rows, cols = self._grid_rows, self._grid_cols
         addr = _lib.lib().tdc_processor_image_buffer(self._h)
-        out = np.empty((rows, cols), dtype=np.complex64)
+        if out is None:
+            out = np.empty((rows, cols), dtype=np.complex64)
+        else:
+            _check_image_array(out, rows, cols)
         if addr and rows * cols:
-            C.memmove(out.ctypes.data, addr, rows * cols * 8)
+            if addr != out.ctypes.data:
+                C.memmove(out.ctypes.data, addr, rows * cols * 8)
         elif rows * cols:
             out[...] = 0  # the reference copies from a buffer that does not exist yet; we return zeros
         return out
@@ -187,6 +201,21 @@ class TdcProcessor:
         n = C.c_int64()
         _lib.check(_lib.lib().tdc_processor_num_pixels(self._h, C.byref(n)))
         return n.value
+
+    def setImageOutput(self, image):
+        """Caller-owned image output: later start() calls write the image straight into
+        ``image`` (C-contiguous complex64 [rows, cols] for the grid set at start), in place
+        from the GPU where it reads and writes host memory coherently, else by one copy.
+        ``None`` returns to the processor's own buffer. The array is kept alive here."""
+        if image is None:
+            _lib.check(_lib.lib().tdc_processor_set_image_output(self._h, None, 0))
+            self._image_out = None
+            return
+        if not isinstance(image, np.ndarray) or image.dtype != np.complex64 or not image.flags.c_contiguous \
+                or not image.flags.writeable:
+            raise ValueError("image output must be a writeable C-contiguous complex64 numpy array")
+        _lib.check(_lib.lib().tdc_processor_set_image_output(self._h, image.ctypes.data, int(image.size) * 2))
+        self._image_out = image
 
     def readsHostMemory(self) -> bool:
         """True when the kernels read the input arrays in place over a coherent host link."""

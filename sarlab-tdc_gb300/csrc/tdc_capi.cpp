@@ -533,6 +533,35 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 }
 
 // Focus the resident acquisition onto the resident grid: image_dev (complex float [P]).
+int processor_use_slot_stream(tdc_processor *p, int priority)
+{
+    TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    for (DevBuf *b : p->device_buffers()) b->release();
+    TDC_CK(cudaStreamSynchronize(p->stream), "stream sync");
+    cudaStream_t st = nullptr;
+    TDC_CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priority), "stream creation");
+    cudaStreamDestroy(p->stream);
+    p->stream = st;
+    for (DevBuf *b : p->device_buffers()) b->alloc_stream = st;
+    return TDC_OK;
+}
+
+void processor_release_memory(tdc_processor *p)
+{
+    for (DevBuf *b : p->device_buffers()) b->release();
+    p->prepared = false;
+    p->plan_path = -1;
+    p->plan_uploaded = false;
+    p->grid_lo_valid = false;
+}
+
+size_t processor_device_bytes(tdc_processor *p)
+{
+    size_t n = 0;
+    for (DevBuf *b : p->device_buffers()) n += b->cap;
+    return n;
+}
+
 int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &launches)
 {
     NvtxRange nvtx("tdc focus");
@@ -637,6 +666,8 @@ int tdc_processor_destroy(tdc_processor *p)
 {
     if (!p) return TDC_OK;
     cudaSetDevice(p->device);
+    // Buffers from the stream-ordered pool go back on the processor's stream before it is destroyed.
+    for (DevBuf *b : p->device_buffers()) b->release();
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (auto &ev : p->ev)
         if (ev) cudaEventDestroy(ev);
@@ -756,6 +787,7 @@ int tdc_processor_start(tdc_processor *p, float doppler_win_center, float dopple
     NvtxRange nvtx("tdc start");
     const auto t0 = std::chrono::steady_clock::now();
     stats_reset(p);
+    p->image_valid = false;
     int launches = 0;
     StartOpts o;
     o.center = doppler_win_center;
@@ -771,15 +803,26 @@ int tdc_processor_start(tdc_processor *p, float doppler_win_center, float dopple
     if (int rc = upload_grid(p, launches)) return rc;
     TDC_CK(cudaEventRecord(p->ev[2], st), "event");
     const long long P = p->P;
-    TDC_CK(p->image_dev.ensure((size_t)P * 8), "alloc image");
+    if (p->image_out && p->image_out_floats < 2 * P)
+        return fail(TDC_ERR_INVALID_ARGUMENT, "image output buffer is smaller than the focus grid");
+    // The reduction writes a caller-owned output in place where the device reads and
+    // writes pageable host memory coherently; otherwise the image goes through device memory.
+    const bool in_place = p->image_out && p->host_reads;
+    if (!in_place) TDC_CK(p->image_dev.ensure((size_t)P * 8), "alloc image");
+    float2 *dst = in_place ? reinterpret_cast<float2 *>(p->image_out) : p->image_dev.as<float2>();
     if (P > 0) {
-        if (int rc = focus_resident(p, p->image_dev.as<float2>(), st, launches)) return rc;
+        if (int rc = focus_resident(p, dst, st, launches)) return rc;
     }
     TDC_CK(cudaEventRecord(p->ev[3], st), "event");
-    TDC_CK(p->image_host.ensure((size_t)P * 8), "alloc host image");
-    if (P > 0) {
-        TDC_CK(cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st),
-               "copy image");
+    size_t d2h = 0;
+    if (!in_place && P > 0) {
+        void *host = p->image_out;
+        if (!host) {
+            TDC_CK(p->image_host.ensure((size_t)P * 8), "alloc host image");
+            host = p->image_host.p;
+        }
+        TDC_CK(cudaMemcpyAsync(host, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st), "copy image");
+        d2h = (size_t)P * 8;
     }
     TDC_CK(cudaEventRecord(p->ev[4], st), "event");
     // tdcprocessor.cpp:149-155: report any asynchronous failure of the launches.
@@ -795,7 +838,7 @@ int tdc_processor_start(tdc_processor *p, float doppler_win_center, float dopple
     p->stats.prep_ms = elapsed(p->ev[1], p->ev[2]);
     p->stats.focus_ms = elapsed(p->ev[2], p->ev[3]);
     p->stats.d2h_ms = elapsed(p->ev[3], p->ev[4]);
-    p->stats.d2h_bytes = (int64_t)P * 8;
+    p->stats.d2h_bytes = (int64_t)d2h;
     p->stats.kernel_launches = launches;
     p->stats.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return TDC_OK;
@@ -804,7 +847,19 @@ int tdc_processor_start(tdc_processor *p, float doppler_win_center, float dopple
 const float *tdc_processor_image_buffer(const tdc_processor *p)
 {
     if (!p || !p->image_valid) return nullptr;
+    if (p->image_out) return p->image_out;
     return static_cast<const float *>(p->image_host.p);
+}
+
+int tdc_processor_set_image_output(tdc_processor *p, float *image_host, int64_t n_floats)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (image_host && n_floats <= 0) return fail(TDC_ERR_INVALID_ARGUMENT, "image output size must be positive");
+    // The image of an earlier start() lives in the buffer it was written to.
+    p->image_valid = false;
+    p->image_out = image_host;
+    p->image_out_floats = image_host ? n_floats : 0;
+    return TDC_OK;
 }
 
 int tdc_processor_grid_shape(const tdc_processor *p, int *n_rows, int *n_cols)

@@ -25,17 +25,24 @@ struct NvtxRange {
     NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
-// Grow-only device buffer.
+// Grow-only device buffer. With alloc_stream set, memory comes from the device's
+// stream-ordered pool (cudaMallocAsync / cudaFreeAsync on that stream), so growing
+// or releasing it does not synchronise the device the way cudaFree does; the owner
+// then releases it before the stream is destroyed.
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
+    cudaStream_t alloc_stream = nullptr;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) {
+            if (alloc_stream) cudaFreeAsync(p, alloc_stream);
+            else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
     }
@@ -44,7 +51,7 @@ struct DevBuf {
         if (bytes == 0) bytes = 16;
         if (bytes <= cap) return cudaSuccess;
         release();
-        cudaError_t e = cudaMalloc(&p, bytes);
+        cudaError_t e = alloc_stream ? cudaMallocAsync(&p, bytes, alloc_stream) : cudaMalloc(&p, bytes);
         if (e == cudaSuccess) cap = bytes;
         else p = nullptr;
         return e;
@@ -168,9 +175,18 @@ struct tdc_processor {
 
     tdc::impl::DevBuf image_dev;
     tdc::impl::PinnedBuf image_host;
+    float *image_out = nullptr;  // caller-owned image output (borrowed), or null
+    int64_t image_out_floats = 0;
     bool image_valid = false;
 
     tdc_start_stats stats{};
+
+    // Every device buffer the processor owns.
+    std::vector<tdc::impl::DevBuf *> device_buffers()
+    {
+        return {&xw,         &chirps,  &skip,    &gs,      &pos_base,    &wr,       &offsets, &flag,
+                &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch, &image_dev};
+    }
 };
 
 namespace tdc {
@@ -196,6 +212,13 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb);
 // Plan units (p->units_host) and make sure the processor's scratch holds them and the partials.
 // max_unit_work > 0 bounds the correlations of one unit (the request loop's granularity).
 int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work = 0.0);
+// Request-loop slots: recreate the processor's stream at `priority` (cudaDeviceGetStreamPriorityRange
+// order) and take its device buffers from the stream-ordered pool on that stream.
+int processor_use_slot_stream(tdc_processor *p, int priority);
+// Give back the processor's device memory (the resident acquisition and grid are dropped).
+void processor_release_memory(tdc_processor *p);
+// Device bytes the processor holds.
+size_t processor_device_bytes(tdc_processor *p);
 
 }  // namespace impl
 }  // namespace tdc

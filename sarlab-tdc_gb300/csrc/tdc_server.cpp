@@ -2,18 +2,22 @@
 // batching of focus jobs with memory-based admission. No reference counterpart
 // (the reference processes one acquisition per blocking start() call).
 //
-// Jobs are submitted from any host thread and run on one GPU:
+// Jobs are submitted from any host thread and run on one GPU. Two host threads
+// serve them:
 //  * priority: least estimated remaining service time first, aged by the time
 //    a job has waited (so short jobs finish fast and long ones are not starved);
-//  * admission: the highest-priority queued job enters when a processor slot is
-//    free and its device footprint fits in the memory budget next to the
-//    resident jobs; its acquisition and grid are copied and prepared on the
-//    slot's own stream while other jobs compute;
-//  * batching: each launch of the focus kernel carries work units (pixel tile x
-//    chirp group, bounded in size) of the active jobs in priority order, later
-//    jobs backfilling what the first leave free, so a job that arrives while
-//    others are on the GPU joins the next launch; at most two launches are
-//    queued so the GPU never waits for the host;
+//  * admission (admission thread): the highest-priority queued job enters when a
+//    processor slot is free and its device footprint fits in the memory budget
+//    next to the resident jobs; its acquisition and grid are copied and prepared
+//    on the slot's own stream, created at the highest stream priority, while
+//    launches run. Slot memory comes from the stream-ordered pool, so growing or
+//    releasing it never synchronises the device;
+//  * batching (launch thread): each launch of the focus kernel carries work units
+//    (pixel tile x chirp group, bounded in size) of the active jobs in priority
+//    order, later jobs backfilling what the first leave free, so a job that
+//    arrives while others are on the GPU joins the next launch. Launches alternate
+//    between two lowest-priority streams, one in flight on each, so a launch's
+//    tail overlaps the next launch and the GPU never waits for the host;
 //  * completion: after the launch holding a job's last units, its partials are
 //    reduced and the image copied back on the same stream; the host collects it
 //    when the job's event completes.
@@ -29,6 +33,7 @@
 #include <cstring>
 #include <deque>
 #include <memory>
+#include <new>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -63,6 +68,7 @@ struct Job {
     size_t n_units = 0;
     double unit_work = 0;  // correlations per unit
     size_t footprint = 0;
+    bool in_place = false;  // the image is written straight into the caller's array (coherent host access)
     int state = kQueued;
     int rc = TDC_OK;
     std::string err;
@@ -111,25 +117,6 @@ size_t device_footprint(const tdc_job_desc &d, int n_sm)
     return b;
 }
 
-size_t slot_bytes(const tdc_processor *p)
-{
-    return p->xw.cap + p->chirps.cap + p->skip.cap + p->gs.cap + p->pos_base.cap + p->wr.cap + p->offsets.cap +
-           p->grid_stage.cap + p->grid_hi.cap + p->grid_lo.cap + p->scratch.cap + p->adj_scratch.cap +
-           p->image_dev.cap;
-}
-
-// Give an idle slot's device memory back (cudaFree synchronises the device, so
-// this runs only when an admission would otherwise exceed the budget).
-void release_slot(tdc_processor *p)
-{
-    for (DevBuf *b : {&p->xw, &p->chirps, &p->skip, &p->gs, &p->pos_base, &p->wr, &p->offsets, &p->grid_stage,
-                      &p->grid_hi, &p->grid_lo, &p->scratch, &p->adj_scratch, &p->image_dev})
-        b->release();
-    p->prepared = false;
-    p->plan_path = -1;
-    p->plan_uploaded = false;
-}
-
 }  // namespace
 
 struct tdc_server {
@@ -142,20 +129,23 @@ struct tdc_server {
 
     std::vector<tdc_processor *> slots;
     std::vector<tdc_processor *> free_slots;
+    std::unordered_map<const tdc_processor *, size_t> slot_mem;  // device bytes each slot holds
+    size_t mem_in_use = 0;
     std::deque<Job *> queue;
+    int admitting = 0;  // jobs taken from the queue whose preparation is under way
     std::vector<Job *> active;
     std::vector<Job *> completing;
     std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;
     uint64_t next_id = 1;
 
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_work, cv_admit, cv_done;
     bool stop = false;
-    std::thread th;
-    int thread_rc = TDC_OK;
-    std::string thread_err;
+    std::thread th_launch, th_admit;
 
-    cudaStream_t compute = nullptr;
+    // Launches alternate between two streams, so the next launch's CTAs take the
+    // SMs that the previous launch's last units leave idle.
+    cudaStream_t compute[2] = {nullptr, nullptr};
     Batch batches[2];
     int next_batch = 0;
     tdc_server_stats stats{};
@@ -169,12 +159,23 @@ struct tdc_server {
         return rem / kRateEstimate - kAging * (t_ms - j->t_submit) / 1e3;
     }
 
-    void loop();
+    void launch_loop();
+    void admit_loop();
     int admit_one(Job *j);
     void launch_batch();
-    void collect();
+    void collect(std::vector<Job *> &finished);
+    void finish_jobs(std::unique_lock<std::mutex> &lk, std::vector<Job *> &finished);
     void fail_job(Job *j, int rc, const std::string &msg);
+    void note_slot_memory(tdc_processor *p);
 };
+
+void tdc_server::note_slot_memory(tdc_processor *p)
+{
+    const size_t now = processor_device_bytes(p);
+    size_t &was = slot_mem[p];
+    mem_in_use = mem_in_use - was + now;
+    was = now;
+}
 
 void tdc_server::fail_job(Job *j, int rc, const std::string &msg)
 {
@@ -187,8 +188,12 @@ void tdc_server::fail_job(Job *j, int rc, const std::string &msg)
         j->slot = nullptr;
     }
     stats.jobs_failed++;
+    cv_done.notify_all();
+    cv_admit.notify_all();
 }
 
+// Copies and prepares a job's acquisition and grid on its slot (the admission
+// thread, without the lock: the slot belongs to the job until it completes).
 int tdc_server::admit_one(Job *j)
 {
     NvtxRange nvtx("tdc server admit");
@@ -211,17 +216,25 @@ int tdc_server::admit_one(Job *j)
     if (!rc) rc = tdc_processor_upload_grid(p);
     if (!rc) rc = focus_plan(p, j->plan, kServerUnitWork);
     if (rc) return rc;
-    if (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess || p->image_host.ensure((size_t)p->P * 8) != cudaSuccess)
+    // Where the device writes pageable host memory coherently, the final reduction
+    // writes the caller's image array directly; otherwise through device + pinned buffers.
+    j->in_place = p->host_reads;
+    if (!j->in_place && (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess ||
+                         p->image_host.ensure((size_t)p->P * 8) != cudaSuccess))
         return set_last_error(TDC_ERR_NO_MEMORY, "image buffers");
+    // The slot's buffers come from the stream-ordered pool on the slot's stream:
+    // settle them before the launch streams use them.
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess) return set_last_error(TDC_ERR_CUDA, "slot stream sync");
     j->n_units = p->units_host.size();
     j->next_unit = 0;
     j->unit_work = (double)kFocusTile * j->plan.job.chirps_per_group * d.n_samples;
     return TDC_OK;
 }
 
-void tdc_server::collect()
+// Finished launches and jobs (lock held). Jobs whose image is done move to
+// `finished`; finish_jobs completes them.
+void tdc_server::collect(std::vector<Job *> &finished)
 {
-    // Launch status words and completed jobs.
     for (Batch &b : batches) {
         if (!b.in_flight || cudaEventQuery(b.ev) != cudaSuccess) continue;
         b.in_flight = false;
@@ -240,8 +253,23 @@ void tdc_server::collect()
             ++i;
             continue;
         }
-        if (j->rc == TDC_OK) {
+        finished.push_back(j);
+        completing.erase(completing.begin() + i);
+    }
+}
+
+// Copies staged images out (without the lock: the jobs' slots stay theirs until
+// they are handed back here) and completes the jobs.
+void tdc_server::finish_jobs(std::unique_lock<std::mutex> &lk, std::vector<Job *> &finished)
+{
+    if (finished.empty()) return;
+    lk.unlock();
+    for (Job *j : finished)
+        if (j->rc == TDC_OK && !j->in_place)
             std::memcpy(j->d.image, j->slot->image_host.p, (size_t)j->d.n_pix * 8);
+    lk.lock();
+    for (Job *j : finished) {
+        if (j->rc == TDC_OK) {
             j->state = kDone;
             stats.jobs_done++;
             stats.correlations += (int64_t)j->d.n_pix * j->d.n_pri * j->d.n_samples;
@@ -252,19 +280,19 @@ void tdc_server::collect()
         j->t_done = now_ms() - t0;
         free_slots.push_back(j->slot);
         j->slot = nullptr;
-        completing.erase(completing.begin() + i);
-        cv_done.notify_all();
     }
+    finished.clear();
+    cv_done.notify_all();
+    cv_admit.notify_all();
 }
 
+// Builds and enqueues the next launch into the free batch (lock held).
 void tdc_server::launch_batch()
 {
     NvtxRange nvtx("tdc server launch");
-    Batch &b = batches[next_batch];
-    if (b.in_flight) {
-        cudaEventSynchronize(b.ev);
-        collect();
-    }
+    const int bi = next_batch;
+    Batch &b = batches[bi];
+    cudaStream_t st = compute[bi];
     // Jobs of this launch in priority order (least remaining service time, aged by the
     // wait): each takes what is left of the launch's work budget and the next ones
     // backfill the rest, so a job that arrives while others run joins the next launch
@@ -314,46 +342,60 @@ void tdc_server::launch_batch()
     FocusJob *hj = reinterpret_cast<FocusJob *>(h + kBatchOffJobs);
     FocusUnit *hu = reinterpret_cast<FocusUnit *>(h + off_units);
     int stage_bytes = 0;
-    size_t u = 0;
     b.finishing.clear();
     b.members = members;
     const double t = now_ms() - t0;
-    for (size_t i = 0; i < members.size(); ++i) {
+    // Units go into the launch longest first, so the launch ends on short units
+    // (its tail then overlaps the next launch on the other stream).
+    std::vector<size_t> order(members.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t c) { return members[a]->unit_work > members[c]->unit_work; });
+    size_t u = 0;
+    for (size_t i : order) {
         Job *j = members[i];
-        hj[i] = j->plan.job;
-        stage_bytes = std::max(stage_bytes, j->plan.stage_bytes);
         for (size_t k = 0; k < take[i]; ++k) {
             FocusUnit fu = j->slot->units_host[j->next_unit + k];
             fu.job = (int)i;
             hu[u++] = fu;
         }
+    }
+    for (size_t i = 0; i < members.size(); ++i) {
+        Job *j = members[i];
+        hj[i] = j->plan.job;
+        stage_bytes = std::max(stage_bytes, j->plan.stage_bytes);
         j->next_unit += take[i];
         if (j->t_first < 0) j->t_first = t;
         if (j->next_unit == j->n_units) b.finishing.push_back(j);
     }
     int err = 0;
-    err |= cudaMemcpyAsync(b.dev.p, b.host.p, bytes, cudaMemcpyHostToDevice, compute) != cudaSuccess;
+    err |= cudaMemcpyAsync(b.dev.p, b.host.p, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess;
     const int bps = focus_fp32_blocks_per_sm(stage_bytes);
     const int grid = (int)std::min<size_t>(n_units, (size_t)std::max(1, n_sm * bps));
     unsigned char *d = static_cast<unsigned char *>(b.dev.p);
     err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
                              reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
-                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, compute) != cudaSuccess;
-    err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, compute) != cudaSuccess;
+                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, st) != cudaSuccess;
+    err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess;
     stats.launches++;
+    if (!b.finishing.empty() && batches[bi ^ 1].in_flight) {
+        // Earlier units of the finishing jobs may be in the launch on the other stream.
+        err |= cudaStreamWaitEvent(st, batches[bi ^ 1].ev, 0) != cudaSuccess;
+    }
     for (Job *j : b.finishing) {
         tdc_processor *p = j->slot;
         const long long P = p->P;
-        err |= launch_focus_reduce(j->plan.job.partial, j->plan.job.n_groups, P, p->image_dev.as<float2>(), compute) !=
-               cudaSuccess;
-        err |= cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, compute) !=
-               cudaSuccess;
-        err |= cudaEventRecord(j->done_ev, compute) != cudaSuccess;
+        float2 *dst = j->in_place ? reinterpret_cast<float2 *>(j->d.image) : p->image_dev.as<float2>();
+        err |= launch_focus_reduce(j->plan.job.partial, j->plan.job.n_groups, P, dst, st) != cudaSuccess;
+        if (!j->in_place)
+            err |= cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st) !=
+                   cudaSuccess;
+        err |= cudaEventRecord(j->done_ev, st) != cudaSuccess;
         j->state = kCompleting;
         completing.push_back(j);
         active.erase(std::find(active.begin(), active.end(), j));
     }
-    err |= cudaEventRecord(b.ev, compute) != cudaSuccess;
+    err |= cudaEventRecord(b.ev, st) != cudaSuccess;
     b.in_flight = true;
     next_batch ^= 1;
     if (err) {
@@ -364,103 +406,123 @@ void tdc_server::launch_batch()
     }
 }
 
-void tdc_server::loop()
+// Admission thread: takes the highest-priority queued job into a free slot when
+// its footprint fits the budget, and prepares it while launches run.
+void tdc_server::admit_loop()
 {
     cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
     for (;;) {
-        // 1. admission (outside the lock for the heavy part)
-        Job *cand = nullptr;
-        {
-            std::unique_lock<std::mutex> lk(mu);
-            collect();
-            if (stop && queue.empty() && active.empty() && completing.empty()) break;
-            size_t in_use = 0;
-            for (tdc_processor *p : slots) in_use += slot_bytes(p);
-            if (!queue.empty() && !free_slots.empty()) {
-                // Queued job with the least estimated remaining service time, aged by its wait.
-                const double t = now_ms() - t0;
-                Job *j = nullptr;
-                for (Job *q : queue)
-                    if (!j || score(q, t) < score(j, t)) j = q;
-                if (j->footprint > budget) {
-                    queue.erase(std::find(queue.begin(), queue.end(), j));
-                    fail_job(j, TDC_ERR_NO_MEMORY, "job needs more device memory than the server budget");
-                    cv_done.notify_all();
-                    continue;
-                }
-                // the free slot that needs the least growth
-                tdc_processor *best = nullptr;
-                size_t best_growth = (size_t)-1;
-                for (tdc_processor *p : free_slots) {
-                    const size_t have = slot_bytes(p);
-                    const size_t growth = j->footprint > have ? j->footprint - have : 0;
-                    if (growth < best_growth) {
-                        best_growth = growth;
-                        best = p;
-                    }
-                }
-                // Idle slots may hold memory from earlier jobs: release the largest first.
-                while (in_use + best_growth > budget) {
-                    tdc_processor *victim = nullptr;
-                    for (tdc_processor *p : free_slots)
-                        if (p != best && slot_bytes(p) > 0 && (!victim || slot_bytes(p) > slot_bytes(victim)))
-                            victim = p;
-                    if (!victim) break;
-                    in_use -= slot_bytes(victim);
-                    release_slot(victim);
-                }
-                if (in_use + best_growth <= budget || (active.empty() && completing.empty())) {
-                    queue.erase(std::find(queue.begin(), queue.end(), j));
-                    free_slots.erase(std::find(free_slots.begin(), free_slots.end(), best));
-                    j->slot = best;
-                    cand = j;
-                }
-            }
-            if (!cand && active.empty()) {
-                if (completing.empty()) {
-                    cv_work.wait_for(lk, std::chrono::milliseconds(2));
-                    continue;
-                }
+        if (stop && queue.empty()) break;
+        if (queue.empty() || free_slots.empty()) {
+            cv_admit.wait_for(lk, std::chrono::milliseconds(5));
+            continue;
+        }
+        // Queued job with the least estimated remaining service time, aged by its wait.
+        const double t = now_ms() - t0;
+        Job *j = nullptr;
+        for (Job *q : queue)
+            if (!j || score(q, t) < score(j, t)) j = q;
+        if (j->footprint > budget) {
+            queue.erase(std::find(queue.begin(), queue.end(), j));
+            fail_job(j, TDC_ERR_NO_MEMORY, "job needs more device memory than the server budget");
+            continue;
+        }
+        // the free slot that needs the least growth
+        tdc_processor *best = nullptr;
+        size_t best_growth = (size_t)-1;
+        for (tdc_processor *p : free_slots) {
+            const size_t have = slot_mem[p];
+            const size_t growth = j->footprint > have ? j->footprint - have : 0;
+            if (growth < best_growth) {
+                best_growth = growth;
+                best = p;
             }
         }
-        if (cand) {
-            cand->t_admit = now_ms() - t0;
-            const int rc = admit_one(cand);
-            std::lock_guard<std::mutex> lk(mu);
-            if (rc) {
-                fail_job(cand, rc, tdc_last_error());
-                cv_done.notify_all();
-            } else if (cand->plan.path != TDC_PATH_FP32_BULK) {
-                // FP64 / general path: not batched, focused on its own.
-                tdc_processor *p = cand->slot;
-                const int rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), compute);
-                if (rc2) {
-                    fail_job(cand, rc2, tdc_last_error());
-                } else {
-                    cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
-                                    compute);
-                    cudaEventRecord(cand->done_ev, compute);
-                    cand->t_first = now_ms() - t0;
-                    cand->state = kCompleting;
-                    completing.push_back(cand);
-                }
-            } else {
-                cand->state = kActive;
-                active.push_back(cand);
+        // Idle slots may hold memory from earlier jobs: release the largest first
+        // (stream-ordered frees: no device synchronisation).
+        while (mem_in_use + best_growth > budget) {
+            tdc_processor *victim = nullptr;
+            for (tdc_processor *p : free_slots)
+                if (p != best && slot_mem[p] > 0 && (!victim || slot_mem[p] > slot_mem[victim])) victim = p;
+            if (!victim) break;
+            processor_release_memory(victim);
+            note_slot_memory(victim);
+        }
+        const bool alone = active.empty() && completing.empty() && admitting == 0;
+        if (mem_in_use + best_growth > budget && !alone) {
+            // wait for a resident job to finish
+            cv_admit.wait_for(lk, std::chrono::milliseconds(5));
+            continue;
+        }
+        queue.erase(std::find(queue.begin(), queue.end(), j));
+        free_slots.erase(std::find(free_slots.begin(), free_slots.end(), best));
+        j->slot = best;
+        j->t_admit = now_ms() - t0;
+        ++admitting;
+        // Reserve the growth now; the slot's real size is noted after preparation.
+        mem_in_use += best_growth;
+        slot_mem[best] += best_growth;
+        lk.unlock();
+        const int rc = admit_one(j);
+        int rc2 = TDC_OK;
+        std::string err2;
+        if (!rc && j->plan.path != TDC_PATH_FP32_BULK) {
+            // FP64 / general path: not batched, focused on its own on the slot's stream.
+            tdc_processor *p = j->slot;
+            rc2 = tdc_processor_focus_device(p, j->in_place ? j->d.image : p->image_dev.as<float>(), p->stream);
+            if (rc2) {
+                err2 = tdc_last_error();
+            } else if ((!j->in_place &&
+                        cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
+                                        p->stream) != cudaSuccess) ||
+                       cudaEventRecord(j->done_ev, p->stream) != cudaSuccess) {
+                rc2 = TDC_ERR_CUDA;
+                err2 = "image copy";
             }
-            continue;  // admit as many as fit before the next launch
         }
-        // 2. keep two launches queued
-        {
-            std::lock_guard<std::mutex> lk(mu);
-            if (!active.empty()) launch_batch();
+        const std::string err = rc ? std::string(tdc_last_error()) : std::string();
+        lk.lock();
+        --admitting;
+        note_slot_memory(j->slot);
+        if (rc) {
+            fail_job(j, rc, err);
+        } else if (rc2) {
+            fail_job(j, rc2, err2);
+        } else if (j->plan.path != TDC_PATH_FP32_BULK) {
+            j->t_first = now_ms() - t0;
+            j->state = kCompleting;
+            completing.push_back(j);
+        } else {
+            j->state = kActive;
+            active.push_back(j);
         }
-        // 3. idle wait for the oldest launch or a completion
-        {
-            Batch &b = batches[next_batch];
-            if (b.in_flight) cudaEventSynchronize(b.ev);
-            else if (!completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(200));
+        cv_work.notify_all();
+    }
+}
+
+// Launch thread: keeps up to two launches in flight (one per stream) and
+// collects finished jobs.
+void tdc_server::launch_loop()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    std::vector<Job *> finished;
+    for (;;) {
+        collect(finished);
+        finish_jobs(lk, finished);
+        const bool any_in_flight = batches[0].in_flight || batches[1].in_flight;
+        if (stop && queue.empty() && admitting == 0 && active.empty() && completing.empty() && !any_in_flight)
+            break;
+        bool pending = false;
+        for (Job *j : active)
+            if (j->next_unit < j->n_units) pending = true;
+        if (pending && !batches[next_batch].in_flight) {
+            launch_batch();
+            continue;
         }
+        // Poll the launches and completions (the lock is free meanwhile).
+        cv_work.wait_for(lk, std::chrono::microseconds(any_in_flight || !completing.empty() ? 200 : 2000));
     }
 }
 
@@ -472,7 +534,8 @@ int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_
     *out = nullptr;
     if (max_jobs <= 0) max_jobs = 32;
     if (cudaSetDevice(device) != cudaSuccess) return set_last_error(TDC_ERR_CUDA, "cudaSetDevice failed");
-    auto s = std::make_unique<tdc_server>();
+    tdc_server *s = new (std::nothrow) tdc_server();
+    if (!s) return set_last_error(TDC_ERR_NO_MEMORY, "out of host memory");
     s->device = device;
     s->max_jobs = std::min(max_jobs, kMaxBatchJobs);
     cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, device);
@@ -484,20 +547,34 @@ int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_
     s->budget = memory_budget_bytes;
     s->batch_work = kServerBatchWork;
     s->t0 = now_ms();
-    if (cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking) != cudaSuccess)
-        return set_last_error(TDC_ERR_CUDA, "stream creation failed");
-    for (Batch &b : s->batches)
-        if (cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming) != cudaSuccess)
-            return set_last_error(TDC_ERR_CUDA, "event creation failed");
-    for (int i = 0; i < s->max_jobs; ++i) {
+    // Launch streams at the lowest priority, slot (preparation) streams at the
+    // highest: when a launch's CTAs retire, a waiting preparation kernel gets the
+    // SM before the next launch's CTAs do.
+    int least = 0, greatest = 0;
+    int rc = TDC_OK;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+        rc = set_last_error(TDC_ERR_CUDA, "stream priority range");
+    for (int i = 0; i < 2 && !rc; ++i)
+        if (cudaStreamCreateWithPriority(&s->compute[i], cudaStreamNonBlocking, least) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->batches[i].ev, cudaEventDisableTiming) != cudaSuccess)
+            rc = set_last_error(TDC_ERR_CUDA, "stream / event creation failed");
+    for (int i = 0; i < s->max_jobs && !rc; ++i) {
         tdc_processor *p = nullptr;
-        if (int rc = tdc_processor_create(device, &p)) return rc;
-        s->slots.push_back(p);
-        s->free_slots.push_back(p);
+        rc = tdc_processor_create(device, &p);
+        if (!rc) {
+            s->slots.push_back(p);
+            s->free_slots.push_back(p);
+            s->slot_mem[p] = 0;
+            rc = processor_use_slot_stream(p, greatest);
+        }
     }
-    tdc_server *raw = s.release();
-    raw->th = std::thread([raw] { raw->loop(); });
-    *out = raw;
+    if (rc) {
+        tdc_server_destroy(s);
+        return rc;
+    }
+    s->th_launch = std::thread([s] { s->launch_loop(); });
+    s->th_admit = std::thread([s] { s->admit_loop(); });
+    *out = s;
     return TDC_OK;
 }
 
@@ -528,7 +605,7 @@ int tdc_server_submit(tdc_server *s, const tdc_job_desc *job, uint64_t *job_id)
     s->queue.push_back(j.get());
     s->jobs.emplace(j->id, std::move(j));
     s->stats.jobs_submitted++;
-    s->cv_work.notify_all();
+    s->cv_admit.notify_all();
     return TDC_OK;
 }
 
@@ -563,10 +640,8 @@ int tdc_server_stats_get(tdc_server *s, tdc_server_stats *out)
     if (!s || !out) return set_last_error(TDC_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     *out = s->stats;
-    size_t in_use = 0;
-    for (tdc_processor *p : s->slots) in_use += slot_bytes(p);
-    out->device_bytes_in_use = (int64_t)in_use;
-    out->queued = (int)s->queue.size();
+    out->device_bytes_in_use = (int64_t)s->mem_in_use;
+    out->queued = (int)s->queue.size() + s->admitting;
     out->active = (int)(s->active.size() + s->completing.size());
     return TDC_OK;
 }
@@ -578,16 +653,23 @@ int tdc_server_destroy(tdc_server *s)
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
         s->cv_work.notify_all();
+        s->cv_admit.notify_all();
     }
-    if (s->th.joinable()) s->th.join();
+    if (s->th_admit.joinable()) s->th_admit.join();
+    if (s->th_launch.joinable()) s->th_launch.join();
     cudaSetDevice(s->device);
-    if (s->compute) cudaStreamSynchronize(s->compute);
+    for (cudaStream_t st : s->compute)
+        if (st) cudaStreamSynchronize(st);
     for (auto &kv : s->jobs)
         if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
-    for (Batch &b : s->batches)
+    for (Batch &b : s->batches) {
         if (b.ev) cudaEventDestroy(b.ev);
+        b.dev.release();
+        b.host.release();
+    }
     for (tdc_processor *p : s->slots) tdc_processor_destroy(p);
-    if (s->compute) cudaStreamDestroy(s->compute);
+    for (cudaStream_t st : s->compute)
+        if (st) cudaStreamDestroy(st);
     delete s;
     return TDC_OK;
 }

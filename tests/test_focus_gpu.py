@@ -297,3 +297,44 @@ def test_in_place_host_reads_match_staged_copies(cuda_device, monkeypatch):
     api["position"] = pos.astype(np.float32)
     _, st_c, _ = run_engine(api, sc.grid, args)
     assert st_c["path_name"] == "general"
+
+
+@pytest.mark.parametrize("host_reads", ["1", "0"])
+def test_image_output_into_caller_buffer(cuda_device, monkeypatch, host_reads):
+    """setImageOutput: start() writes into the caller's array (in place from the GPU where it
+    reads and writes host memory, else by one copy); the image equals the default buffer's."""
+    import _sarlabtdc
+
+    if host_reads == "0":
+        monkeypatch.setenv("TDC_GB300_HOST_READS", "0")
+    sc = scenes.small_scene(seed=17, n_pri=200, n_samples=64, nx=23, ny=17, device="cuda")
+    api = sc.api_arrays()
+    args = (0.0, INF, False, True, True)
+    ref, _, _ = run_engine(api, sc.grid, args)
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                 api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+    p.setFocusGrid(sc.grid)
+    out = np.full(ref.shape, np.complex64(7 + 7j))
+    p.setImageOutput(out)
+    p.start(*args)
+    np.testing.assert_array_equal(out, ref)
+    st = p.lastStats()
+    if p.readsHostMemory():
+        assert st["d2h_bytes"] == 0
+    else:
+        assert st["d2h_bytes"] == ref.size * 8
+    assert p.getFocusedImage() is not out and np.array_equal(p.getFocusedImage(), ref)
+    again = np.empty_like(ref)
+    assert p.getFocusedImage(out=again) is again and np.array_equal(again, ref)
+    # a buffer smaller than the grid is refused at start(), before any write
+    small = np.zeros((2, 2), np.complex64)
+    p.setImageOutput(small)
+    with pytest.raises(ValueError):
+        p.start(*args)
+    assert np.all(small == 0)
+    p.setImageOutput(None)
+    p.start(*args)
+    np.testing.assert_array_equal(p.getFocusedImage(), ref)
+    with pytest.raises(ValueError):
+        p.setImageOutput(np.zeros((4, 4), np.complex128))
