@@ -138,7 +138,10 @@ typedef struct tdc_start_stats {
 typedef enum tdc_path {
     TDC_PATH_FP32_BULK = 0,    /* per-chirp trajectory, uniform sample spacing */
     TDC_PATH_FP64_PHASE = 1,   /* comparator, per-chirp trajectory */
-    TDC_PATH_GENERAL = 2       /* per-sample trajectory or non-uniform sample times */
+    TDC_PATH_GENERAL = 2,      /* per-sample trajectory / window or non-uniform sample times: FP32 phasors
+                                  with a double-float range at sample 0 and per-sample corrections */
+    TDC_PATH_GENERAL_FP64 = 3  /* the same inputs with FP64 phase per sample (FP64 precision, or intra-chirp
+                                  motion too large for the FP32 correction, or rows too long to stage) */
 } tdc_path;
 
 int tdc_processor_last_stats(const tdc_processor *proc, tdc_start_stats *out);
@@ -200,7 +203,9 @@ int tdc_processor_reads_host_memory(const tdc_processor *proc);
  * image_host. The buffer is borrowed until it is replaced or the processor is
  * destroyed. Where the device accesses pageable host memory coherently
  * (tdc_processor_reads_host_memory() = 1) the final reduction kernel writes it
- * in place, with no device-to-host copy; otherwise the image is copied into it.
+ * in place, with no device-to-host copy (fastest for an array the host has already
+ * written: a never-touched allocation takes its first-touch page faults on the GPU);
+ * otherwise the image is copied into it.
  * n_floats must be >= 2 x the pixels of the grid at start(); image_host = NULL
  * returns to the processor's own buffer. */
 int tdc_processor_set_image_output(tdc_processor *proc, float *image_host, int64_t n_floats);

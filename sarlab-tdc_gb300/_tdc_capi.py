@@ -24,7 +24,7 @@ TDC_ERR_SHAPE = -7
 PRECISION_FP32_BULK = 0
 PRECISION_FP64_PHASE = 1
 
-PATH_NAMES = {0: "fp32_bulk", 1: "fp64_phase", 2: "general"}
+PATH_NAMES = {0: "fp32_bulk", 1: "fp64_phase", 2: "general", 3: "general_fp64"}
 
 
 class NoallocFocusArgs(C.Structure):

@@ -80,6 +80,10 @@ float window_centre(const float *vel, const float *att, const float *bore, float
 
 // Phase tolerance for treating the sample frequencies as affine in the sample index.
 constexpr double kUniformPhaseTolRad = 1e-4;
+// FP32 general kernel: largest |(R_s^2 - R0^2) / R0^2| its range-change series takes, and
+// the bytes of chirp rows per pipeline stage it aims for.
+constexpr double kGeneralMaxEps = 0.1;
+constexpr int kGeneralStageTarget = 32768;
 
 }  // namespace impl
 }  // namespace tdc
@@ -159,25 +163,30 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     // Trajectory element of (chirp c, sample s): per-sample arrays, or one row per chirp.
     const bool tpc = p->traj_per_chirp;
     auto ti = [tpc, S](long c, long s) -> size_t { return tpc ? (size_t)c : (size_t)c * S + s; };
+    bool pos_differ = false, motion_differ = false;
     if (tpc) {
         p->per_chirp = true;
     } else if (p->host_reads) {
         // The device reads the caller's per-sample arrays in place (coherent host access)
-        // and reports whether any chirp's samples differ.
-        TDC_CK(p->flag.ensure(16), "alloc flag");
-        TDC_CK(cudaMemsetAsync(p->flag.p, 0, 4, p->stream), "reset flag");
-        if (!p->pos64) TDC_CK(launch_rows_differ(p->pos, C, S, 3, p->flag.as<int>(), p->stream), "scan kernel");
-        if (p->vel) TDC_CK(launch_rows_differ(p->vel, C, S, 3, p->flag.as<int>(), p->stream), "scan kernel");
-        if (p->att) TDC_CK(launch_rows_differ(p->att, C, S, 4, p->flag.as<int>(), p->stream), "scan kernel");
-        int differ = 0;
-        TDC_CK(cudaMemcpyAsync(&differ, p->flag.p, 4, cudaMemcpyDeviceToHost, p->stream), "read flag");
+        // and reports whether any chirp's samples differ: flag[0] positions, flag[1] velocity
+        // or attitude.
+        TDC_CK(p->flag.ensure(64), "alloc flag");
+        int *flag = p->flag.as<int>();
+        TDC_CK(cudaMemsetAsync(flag, 0, 8, p->stream), "reset flag");
+        if (!p->pos64) TDC_CK(launch_rows_differ(p->pos, C, S, 3, flag, p->stream), "scan kernel");
+        if (p->vel) TDC_CK(launch_rows_differ(p->vel, C, S, 3, flag + 1, p->stream), "scan kernel");
+        if (p->att) TDC_CK(launch_rows_differ(p->att, C, S, 4, flag + 1, p->stream), "scan kernel");
+        int differ[2] = {0, 0};
+        TDC_CK(cudaMemcpyAsync(differ, flag, 8, cudaMemcpyDeviceToHost, p->stream), "read flag");
         TDC_CK(cudaStreamSynchronize(p->stream), "scan sync");
-        p->per_chirp = differ == 0;
+        pos_differ = differ[0] != 0;
+        motion_differ = differ[1] != 0;
         launches += (!p->pos64) + (p->vel != nullptr) + (p->att != nullptr);
     } else {
-        p->per_chirp = (p->pos64 || rows_constant(p->pos, C, S, 3)) && rows_constant(p->vel, C, S, 3) &&
-                       rows_constant(p->att, C, S, 4);
+        pos_differ = !p->pos64 && !rows_constant(p->pos, C, S, 3);
+        motion_differ = !rows_constant(p->vel, C, S, 3) || !rows_constant(p->att, C, S, 4);
     }
+    if (!tpc) p->per_chirp = !pos_differ && !motion_differ;
     fit_frequencies(p->sample_times, S, p->start_freq, p->mod_rate, p->F0, p->F1, p->resid_hz);
     for (int k = 0; k < 3; ++k) {
         p->ant_min[k] = std::numeric_limits<double>::infinity();
@@ -230,6 +239,52 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         }
     }
 
+    // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
+    const int s_pad = (int)round_up((size_t)S, kSampleAlign);
+    const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
+    std::vector<float> gres(s_pad, 0.f);
+    for (int s = 0; s < S; ++s) {
+        const double gsv = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
+        gres[s] = (float)(gsv - (g0 + g1 * s));
+    }
+    std::vector<ChirpRec> rec0;
+    std::vector<float4> traj, wins;
+    p->traj_varies = pos_differ;
+    p->delta_max = 0.0;
+    bool any_velocity = false;
+    if (!p->per_chirp) {
+        rec0.resize(C);
+        for (int c = 0; c < C; ++c) rec0[c] = recs[(size_t)c * S];
+        for (size_t i = 0; i < (size_t)C * S && p->vel && !any_velocity; ++i)
+            any_velocity = p->vel[3 * i] != 0.f || p->vel[3 * i + 1] != 0.f || p->vel[3 * i + 2] != 0.f;
+    }
+    // The window can change within a chirp when the band is finite and either the motion
+    // varies per sample or a moving antenna's direction to the pixel does.
+    p->win_varies = !p->per_chirp && std::isfinite(o.bw) && (motion_differ || (pos_differ && any_velocity));
+    if (p->traj_varies) {
+        traj.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+        double d2max = 0.0;
+        for (int c = 0; c < C; ++c) {
+            const float *p0 = p->pos + 3 * ti(c, 0);
+            for (int s = 0; s < S; ++s) {
+                const float *ps = p->pos + 3 * ti(c, s);
+                const double dx = (double)ps[0] - p0[0], dy = (double)ps[1] - p0[1], dz = (double)ps[2] - p0[2];
+                d2max = std::max(d2max, dx * dx + dy * dy + dz * dz);
+                const double gsv = g0 + g1 * s + (double)gres[s];
+                traj[(size_t)c * s_pad + s] = make_float4((float)dx, (float)dy, (float)dz, (float)gsv);
+            }
+        }
+        p->delta_max = std::sqrt(d2max);
+    }
+    if (p->win_varies) {
+        wins.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int c = 0; c < C; ++c)
+            for (int s = 0; s < S; ++s) {
+                const ChirpRec &r = recs[(size_t)c * S + s];
+                wins[(size_t)c * s_pad + s] = make_float4(r.vel.x, r.vel.y, r.vel.z, r.p_hi.w);
+            }
+    }
+
     // ---- skip-test points (tdcprocessor.cpp:347-383, stale staging rows included) ----
     const int n_chunks = (C + kChunk - 1) / kChunk;
     std::vector<SkipPoint> skip((size_t)n_chunks * 9);
@@ -275,7 +330,6 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         gs[s] = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
 
     // ---- device buffers ----
-    const int s_pad = (int)round_up((size_t)S, kSampleAlign);
     p->s_pad = s_pad;
     p->n_chunks = n_chunks;
     cudaStream_t st = p->stream;
@@ -298,6 +352,26 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(cudaMemcpyAsync(p->gs.p, gs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "copy freq table");
     TDC_CK(cudaMemcpyAsync(p->pos_base.p, base.data(), (size_t)C * 24, cudaMemcpyHostToDevice, st),
            "copy base positions");
+    TDC_CK(p->gres.ensure((size_t)s_pad * 4), "alloc residual frequency table");
+    TDC_CK(cudaMemcpyAsync(p->gres.p, gres.data(), (size_t)s_pad * 4, cudaMemcpyHostToDevice, st),
+           "copy residual frequency table");
+    if (!rec0.empty()) {
+        TDC_CK(p->gen_rec.ensure(rec0.size() * sizeof(ChirpRec)), "alloc sample-0 records");
+        TDC_CK(cudaMemcpyAsync(p->gen_rec.p, rec0.data(), rec0.size() * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
+               "copy sample-0 records");
+    }
+    if (!traj.empty()) {
+        TDC_CK(p->traj.ensure(traj.size() * sizeof(float4)), "alloc per-sample offsets");
+        TDC_CK(cudaMemcpyAsync(p->traj.p, traj.data(), traj.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
+               "copy per-sample offsets");
+    }
+    if (!wins.empty()) {
+        TDC_CK(p->wins.ensure(wins.size() * sizeof(float4)), "alloc per-sample windows");
+        TDC_CK(cudaMemcpyAsync(p->wins.p, wins.data(), wins.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
+               "copy per-sample windows");
+    }
+    p->stats.h2d_bytes += (int64_t)s_pad * 4 + (int64_t)(rec0.size() * sizeof(ChirpRec)) +
+                          (int64_t)((traj.size() + wins.size()) * sizeof(float4));
     p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)n_rec * sizeof(ChirpRec) +
                           (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
@@ -381,17 +455,51 @@ int upload_grid(tdc_processor *p, int &launches)
     return TDC_OK;
 }
 
-int choose_path(const tdc_processor *p)
+int general_variant(const tdc_processor *p)
 {
-    if (!p->per_chirp) return TDC_PATH_GENERAL;
     const double rmax = max_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
     const double dev = 2.0 * M_PI * 2.0 * p->resid_hz * rmax / kC0;
-    if (dev > kUniformPhaseTolRad) return TDC_PATH_GENERAL;
-    if (p->precision == TDC_PRECISION_FP64_PHASE) return TDC_PATH_FP64_PHASE;
-    if (focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)p->s_pad * 8 + sizeof(ChirpRec), 128) >
-        227 * 1024)
-        return TDC_PATH_GENERAL;
-    return TDC_PATH_FP32_BULK;
+    return (p->traj_varies ? 1 : 0) | (p->win_varies ? 2 : 0) | (dev > kUniformPhaseTolRad ? 4 : 0);
+}
+
+// Smallest distance between the antenna positions' bounding box and the grid's.
+double min_range(const double *amin, const double *amax, const double *gmin, const double *gmax)
+{
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        const double d = std::max({0.0, gmin[k] - amax[k], amin[k] - gmax[k]});
+        r2 += d * d;
+    }
+    return std::sqrt(r2);
+}
+
+int choose_path(const tdc_processor *p)
+{
+    const int variant = general_variant(p);
+    const bool fp64 = p->precision == TDC_PRECISION_FP64_PHASE;
+    if (variant == 0) {
+        // One record per chirp describes every sample (a per-sample trajectory whose
+        // variation cannot change the phase or the window is focused like a per-chirp one).
+        if (fp64) return p->per_chirp ? TDC_PATH_FP64_PHASE : TDC_PATH_GENERAL_FP64;
+        if (focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)p->s_pad * 8 + sizeof(ChirpRec), 128) >
+            227 * 1024)
+            return TDC_PATH_GENERAL_FP64;
+        return TDC_PATH_FP32_BULK;
+    }
+    if (fp64) return TDC_PATH_GENERAL_FP64;
+    if (variant & 1) {
+        // Per-sample range change d_s = N/(2 R0) f(N/R0^2): the series of f stays accurate for
+        // |N/R0^2| <= 2 dmax/Rmin + (dmax/Rmin)^2 <= 0.1.
+        const double rmin = min_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
+        if (!(rmin > 0.0)) return TDC_PATH_GENERAL_FP64;
+        const double q = p->delta_max / rmin;
+        if (2.0 * q + q * q > kGeneralMaxEps) return TDC_PATH_GENERAL_FP64;
+    }
+    int cb = 1;
+    const int stage_bytes = general_stage_bytes_for(p->s_pad, variant, cb);
+    // 227 KiB of shared memory per CTA, less the kernel's static shared memory
+    if (focus_general_smem_bytes(stage_bytes, p->s_pad) > 226 * 1024) return TDC_PATH_GENERAL_FP64;
+    return TDC_PATH_GENERAL;
 }
 
 // Split the chirps into groups so that tiles x groups units fill whole waves of `slots`.
@@ -440,13 +548,25 @@ int stage_bytes_for(int s_pad, int &cb)
     return (int)round_up((size_t)cb * row, 128);
 }
 
+int general_stage_bytes_for(int s_pad, int variant, int &cb)
+{
+    const int row = s_pad * (8 + ((variant & 1) ? 16 : 0) + ((variant & 2) ? 16 : 0)) + (int)sizeof(ChirpRec);
+    cb = std::max(1, kGeneralStageTarget / row);
+    return (int)round_up((size_t)cb * row, 128);
+}
+
 // Job record of the resident acquisition x resident grid under the current plan.
-FocusJob make_job(const tdc_processor *p, float4 *partial, int cb)
+FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
 {
     FocusJob job;
     std::memset(&job, 0, sizeof(job));
     job.xw = p->xw.as<const float4>();
-    job.chirps = p->chirps.as<const ChirpRec>();
+    // FP32 kernels read one record per chirp; the FP64 general kernel one per sample.
+    const bool rec_per_sample = !p->per_chirp && path == TDC_PATH_GENERAL_FP64;
+    job.chirps = p->per_chirp || rec_per_sample ? p->chirps.as<const ChirpRec>() : p->gen_rec.as<const ChirpRec>();
+    job.traj = p->traj_varies ? p->traj.as<const float4>() : nullptr;
+    job.wins = p->win_varies ? p->wins.as<const float4>() : nullptr;
+    job.gres = p->gres.as<const float>();
     job.grid_hi = p->grid_hi.as<const float4>();
     job.grid_lo = p->grid_lo_valid ? p->grid_lo.as<const float4>() : nullptr;
     job.skip = p->skip.as<const SkipPoint>();
@@ -462,7 +582,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb)
     job.stage_chirps = cb;
     job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
     job.n_tiles = (int)((p->P + kFocusTile - 1) / kFocusTile);
-    job.per_sample = p->per_chirp ? 0 : 1;
+    job.per_sample = rec_per_sample ? 1 : 0;
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
     split_dd(g0, job.g0_hi, job.g0_lo);
     split_dd(g1, job.g1, job.g1_lo);
@@ -482,11 +602,17 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     const int C = p->C;
 
     int cb = 1;
-    const int stage_bytes = stage_bytes_for(p->s_pad, cb);
+    const int variant = path == TDC_PATH_GENERAL ? general_variant(p) : 0;
+    const int stage_bytes =
+        path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, cb) : stage_bytes_for(p->s_pad, cb);
     int slots;
     if (path == TDC_PATH_FP32_BULK) {
         const int bps = focus_fp32_blocks_per_sm(stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
+        slots = p->n_sm * bps;
+    } else if (path == TDC_PATH_GENERAL) {
+        const int bps = focus_general_blocks_per_sm(variant, stage_bytes, p->s_pad);
+        if (bps <= 0) return fail(TDC_ERR_CUDA, "general focus kernel does not fit on the device");
         slots = p->n_sm * bps;
     } else {
         slots = p->n_sm * 4;
@@ -523,12 +649,13 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     }
     unsigned char *scr = p->scratch.as<unsigned char>();
     plan.path = path;
+    plan.variant = variant;
     plan.cb = cb;
     plan.stage_bytes = stage_bytes;
     plan.slots = slots;
     plan.off_job = L.off_job;
     plan.off_units = L.off_units;
-    plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb);
+    plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
     return TDC_OK;
 }
 
@@ -593,9 +720,13 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
         const int grid = std::min(n_units, slots);
         TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, st),
                "focus kernel");
+    } else if (path == TDC_PATH_GENERAL) {
+        const int grid = std::min(n_units, slots);
+        TDC_CK(launch_focus_general(plan.variant, jobs_dev, units_dev, n_units, counter, status, stage_bytes,
+                                    p->s_pad, grid, st),
+               "focus kernel (general)");
     } else {
-        TDC_CK(launch_focus_fp64(jobs_dev, units_dev, n_units, status, p->per_chirp ? 0 : 1, st),
-               "focus kernel (fp64)");
+        TDC_CK(launch_focus_fp64(jobs_dev, units_dev, n_units, status, job.per_sample, st), "focus kernel (fp64)");
     }
     TDC_CK(launch_focus_reduce(job.partial, p->plan_groups, P, image_dev, st), "reduce kernel");
     launches += 2;
@@ -961,7 +1092,7 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
     if (p->P <= 0) return fail(TDC_ERR_STATE, "no focus grid");
     if (!grad_image_dev || !grad_offsets_dev) return fail(TDC_ERR_INVALID_ARGUMENT, "null gradient buffer");
-    if (choose_path(p) != TDC_PATH_FP32_BULK)
+    if (!p->per_chirp || choose_path(p) != TDC_PATH_FP32_BULK)
         return fail(TDC_ERR_UNSUPPORTED, "the adjoint needs the FP32-bulk path (per-chirp trajectory, uniform "
                                          "sample spacing)");
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
@@ -986,7 +1117,7 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     const size_t total = off_gpart + (size_t)n_tiles * C * 16;
     TDC_CK(p->adj_scratch.ensure(total), "alloc adjoint scratch");
     unsigned char *scr = p->adj_scratch.as<unsigned char>();
-    FocusJob job = make_job(p, nullptr, cb);
+    FocusJob job = make_job(p, nullptr, cb, TDC_PATH_FP32_BULK);
     job.n_groups = n_groups;
     job.chirps_per_group = cpg;
     TDC_CK(cudaMemcpyAsync(scr + off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");

@@ -28,6 +28,11 @@ constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows
 #define TDC_FOCUS_STAGE_TARGET 16640
 #endif
 constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp rows + records per pipeline stage
+// Pixels per thread of the FP32 general kernel (per-sample trajectories / windows, non-uniform sampling).
+#ifndef TDC_GENERAL_PT
+#define TDC_GENERAL_PT 4
+#endif
+constexpr int kGeneralPT = TDC_GENERAL_PT;
 
 // One chirp's trajectory record, 48 bytes (3 x float4):
 //   p_hi.xyz  antenna position, high float of a double-float pair; p_hi.w = Doppler window centre [Hz]
@@ -60,6 +65,9 @@ struct FocusJob {
     const float4 *grid_lo;   // [P] or nullptr
     const SkipPoint *skip;   // [n_chunks][9]
     const double *gs;        // [S] 2 f_s / c0 (FP64 kernels only)
+    const float4 *traj;      // [C][s_pad] (P[c,s] - P[c,0], 2 f_s / c0) (FP32 general kernel, per-sample positions)
+    const float4 *wins;      // [C][s_pad] (velocity, window centre) per sample (FP32 general kernel, per-sample windows)
+    const float *gres;       // [s_pad] 2 f_s / c0 - (g0 + g1 s) (FP32 general kernel, non-uniform sampling)
     float4 *partial;         // [n_groups][P]: (sum.re, sum.im, comp.re, comp.im)
     long long P;
     int C;
@@ -80,6 +88,10 @@ struct FocusJob {
     float az_a;              // azimuth window a
     float g1_lo;             // low part of g1 (double-float pair)
 };
+
+// Kernels copy a FocusJob into shared memory one int per thread (128 threads); the
+// no-allocation scratch reserves 256 bytes for it.
+static_assert(sizeof(FocusJob) <= 256 && sizeof(FocusJob) % 8 == 0, "FocusJob layout");
 
 struct FocusUnit {
     int job;
@@ -114,6 +126,13 @@ cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_d
                               int *status_dev, int per_sample, cudaStream_t st);
 cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image,
                                 cudaStream_t st);
+// FP32 general focus (tdc_general.cu). variant bits: 1 per-sample positions, 2 per-sample
+// windows, 4 non-uniform sampling (at least one set).
+cudaError_t launch_focus_general(int variant, const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
+                                 int *counter_dev, int *status_dev, int stage_bytes, int s_pad, int grid_ctas,
+                                 cudaStream_t st);
+int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad);
+int focus_general_smem_bytes(int stage_bytes, int s_pad);
 
 // Adjoint of the FP32-bulk focus w.r.t. per-chirp position offsets: per-(tile, chirp)
 // float4 partials, then an FP64 sum over tiles into grad[C][3].

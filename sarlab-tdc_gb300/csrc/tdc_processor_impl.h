@@ -151,10 +151,16 @@ struct tdc_processor {
     bool prepared = false;
     tdc::impl::StartOpts opts;
     bool per_chirp = true;
+    bool traj_varies = false;   // positions differ within a chirp (FP32 per-sample positions)
+    bool win_varies = false;    // the Doppler window can differ within a chirp (finite band, per-sample motion)
+    double delta_max = 0.0;     // max |P[c,s] - P[c,0]| [m]
     double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
     double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
     int s_pad = 0, n_chunks = 0;
     tdc::impl::DevBuf xw, chirps, skip, gs, pos_base, wr, offsets, flag;
+    // FP32 general path: sample-0 records per chirp (when chirps holds one per sample),
+    // per-sample offsets / windows, residual frequency table.
+    tdc::impl::DevBuf gen_rec, traj, wins, gres;
 
     // Device grid.
     long long P = 0;
@@ -184,8 +190,9 @@ struct tdc_processor {
     // Every device buffer the processor owns.
     std::vector<tdc::impl::DevBuf *> device_buffers()
     {
-        return {&xw,         &chirps,  &skip,    &gs,      &pos_base,    &wr,       &offsets, &flag,
-                &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch, &image_dev};
+        return {&xw,      &chirps,     &skip,    &gs,      &pos_base, &wr,      &offsets,     &flag,     &gen_rec,
+                &traj,    &wins,       &gres,    &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch,
+                &image_dev};
     }
 };
 
@@ -195,6 +202,7 @@ namespace impl {
 // Work plan of one focus of a processor's resident acquisition onto its resident grid.
 struct FocusPlan {
     int path = 0;         // tdc_path
+    int variant = 0;      // FP32 general kernel variant bits (TDC_PATH_GENERAL)
     int cb = 1;           // chirps per pipeline stage
     int stage_bytes = 0;  // bytes per pipeline stage
     int slots = 0;        // resident CTAs of the kernel on the device
@@ -208,7 +216,11 @@ int upload_grid(tdc_processor *p, int &launches);
 int choose_path(const tdc_processor *p);
 void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg);
 int stage_bytes_for(int s_pad, int &cb);
-FocusJob make_job(const tdc_processor *p, float4 *partial, int cb);
+// Stage bytes of the FP32 general kernel for a variant (bit 1 per-sample positions, 2 windows).
+int general_stage_bytes_for(int s_pad, int variant, int &cb);
+// Variant bits of the FP32 general kernel for the resident acquisition.
+int general_variant(const tdc_processor *p);
+FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path);
 // Plan units (p->units_host) and make sure the processor's scratch holds them and the partials.
 // max_unit_work > 0 bounds the correlations of one unit (the request loop's granularity).
 int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work = 0.0);

@@ -68,7 +68,6 @@ struct Job {
     size_t n_units = 0;
     double unit_work = 0;  // correlations per unit
     size_t footprint = 0;
-    bool in_place = false;  // the image is written straight into the caller's array (coherent host access)
     int state = kQueued;
     int rc = TDC_OK;
     std::string err;
@@ -216,11 +215,10 @@ int tdc_server::admit_one(Job *j)
     if (!rc) rc = tdc_processor_upload_grid(p);
     if (!rc) rc = focus_plan(p, j->plan, kServerUnitWork);
     if (rc) return rc;
-    // Where the device writes pageable host memory coherently, the final reduction
-    // writes the caller's image array directly; otherwise through device + pinned buffers.
-    j->in_place = p->host_reads;
-    if (!j->in_place && (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess ||
-                         p->image_host.ensure((size_t)p->P * 8) != cudaSuccess))
+    // Images go through device + pinned buffers: a kernel writing the caller's freshly
+    // allocated (untouched) pages directly would take the page faults on the GPU while
+    // other jobs' launches run.
+    if (p->image_dev.ensure((size_t)p->P * 8) != cudaSuccess || p->image_host.ensure((size_t)p->P * 8) != cudaSuccess)
         return set_last_error(TDC_ERR_NO_MEMORY, "image buffers");
     // The slot's buffers come from the stream-ordered pool on the slot's stream:
     // settle them before the launch streams use them.
@@ -265,8 +263,7 @@ void tdc_server::finish_jobs(std::unique_lock<std::mutex> &lk, std::vector<Job *
     if (finished.empty()) return;
     lk.unlock();
     for (Job *j : finished)
-        if (j->rc == TDC_OK && !j->in_place)
-            std::memcpy(j->d.image, j->slot->image_host.p, (size_t)j->d.n_pix * 8);
+        if (j->rc == TDC_OK) std::memcpy(j->d.image, j->slot->image_host.p, (size_t)j->d.n_pix * 8);
     lk.lock();
     for (Job *j : finished) {
         if (j->rc == TDC_OK) {
@@ -385,11 +382,10 @@ void tdc_server::launch_batch()
     for (Job *j : b.finishing) {
         tdc_processor *p = j->slot;
         const long long P = p->P;
-        float2 *dst = j->in_place ? reinterpret_cast<float2 *>(j->d.image) : p->image_dev.as<float2>();
-        err |= launch_focus_reduce(j->plan.job.partial, j->plan.job.n_groups, P, dst, st) != cudaSuccess;
-        if (!j->in_place)
-            err |= cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st) !=
-                   cudaSuccess;
+        err |= launch_focus_reduce(j->plan.job.partial, j->plan.job.n_groups, P, p->image_dev.as<float2>(), st) !=
+               cudaSuccess;
+        err |= cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st) !=
+               cudaSuccess;
         err |= cudaEventRecord(j->done_ev, st) != cudaSuccess;
         j->state = kCompleting;
         completing.push_back(j);
@@ -470,12 +466,11 @@ void tdc_server::admit_loop()
         if (!rc && j->plan.path != TDC_PATH_FP32_BULK) {
             // FP64 / general path: not batched, focused on its own on the slot's stream.
             tdc_processor *p = j->slot;
-            rc2 = tdc_processor_focus_device(p, j->in_place ? j->d.image : p->image_dev.as<float>(), p->stream);
+            rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), p->stream);
             if (rc2) {
                 err2 = tdc_last_error();
-            } else if ((!j->in_place &&
-                        cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
-                                        p->stream) != cudaSuccess) ||
+            } else if (cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
+                                       p->stream) != cudaSuccess ||
                        cudaEventRecord(j->done_ev, p->stream) != cudaSuccess) {
                 rc2 = TDC_ERR_CUDA;
                 err2 = "image copy";
