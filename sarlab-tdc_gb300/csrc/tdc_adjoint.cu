@@ -333,8 +333,7 @@ int adjoint_fp32_smem_bytes(int stage_bytes, int stage_chirps)
 int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps)
 {
     const int smem = adjoint_fp32_smem_bytes(stage_bytes, stage_chirps);
-    if (cudaFuncSetAttribute(adjoint_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-        return 0;
+    if (allow_max_dynamic_smem(adjoint_fp32_kernel) != cudaSuccess) return 0;
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_fp32_kernel, kFocusThreads, smem) !=
         cudaSuccess)
@@ -347,7 +346,7 @@ cudaError_t launch_adjoint_fp32(const FocusJob *jobs_dev, const FocusUnit *units
                                 const float2 *gimg, float4 *gpart, cudaStream_t st)
 {
     const int smem = adjoint_fp32_smem_bytes(stage_bytes, stage_chirps);
-    cudaError_t e = cudaFuncSetAttribute(adjoint_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = allow_max_dynamic_smem(adjoint_fp32_kernel);
     if (e != cudaSuccess) return e;
     adjoint_fp32_kernel<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
                                                                  status_dev, stage_bytes, gimg, gpart);

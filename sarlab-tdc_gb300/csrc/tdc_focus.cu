@@ -340,10 +340,7 @@ int focus_fp32_smem_bytes(int stage_bytes)
 int focus_fp32_blocks_per_sm(int stage_bytes)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    if (cudaFuncSetAttribute(focus_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-        cudaSuccess) {
-        return 0;
-    }
+    if (allow_max_dynamic_smem(focus_fp32_kernel) != cudaSuccess) return 0;
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel, kFocusThreads, smem) !=
         cudaSuccess) {
@@ -356,7 +353,7 @@ cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_d
                               int *status_dev, int stage_bytes, int grid_ctas, cudaStream_t st)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    cudaError_t e = cudaFuncSetAttribute(focus_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel);
     if (e != cudaSuccess) return e;
     focus_fp32_kernel<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
                                                                status_dev, stage_bytes);

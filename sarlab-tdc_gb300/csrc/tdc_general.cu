@@ -384,7 +384,7 @@ int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad)
     KernelFn fn = select_kernel(variant);
     if (!fn) return 0;
     const int smem = focus_general_smem_bytes(stage_bytes, s_pad);
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+    if (allow_max_dynamic_smem(fn) != cudaSuccess) return 0;
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kT, smem) != cudaSuccess) return 0;
     return blocks;
@@ -397,7 +397,7 @@ cudaError_t launch_focus_general(int variant, const FocusJob *jobs_dev, const Fo
     KernelFn fn = select_kernel(variant);
     if (!fn) return cudaErrorInvalidValue;
     const int smem = focus_general_smem_bytes(stage_bytes, s_pad);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = allow_max_dynamic_smem(fn);
     if (e != cudaSuccess) return e;
     fn<<<grid_ctas, kT, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev, status_dev, stage_bytes);
     return cudaGetLastError();

@@ -143,6 +143,23 @@ cudaError_t launch_adjoint_reduce(const float4 *gpart, int n_tiles, int C, doubl
 int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps);
 int adjoint_fp32_smem_bytes(int stage_bytes, int stage_chirps);
 
+// Let `fn` launch with as much dynamic shared memory as the device allows. The attribute
+// is process-wide per kernel: every caller sets this same value, so threads that plan
+// and launch with different sizes at the same time cannot undercut one another.
+template <class F>
+inline cudaError_t allow_max_dynamic_smem(F *fn)
+{
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes a{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, reinterpret_cast<const void *>(fn));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(reinterpret_cast<const void *>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int)a.sharedSizeBytes);
+    return e;
+}
+
 // Record `msg` as the calling thread's tdc_last_error() and return `code`.
 int set_last_error(int code, const char *msg);
 inline int set_last_error(int code, const std::string &msg) { return set_last_error(code, msg.c_str()); }
