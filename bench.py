@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--quick", action="store_true", help="skip plain / e2e / CPU legs")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the oracle accuracy check")
+    ap.add_argument("--general-only", action="store_true",
+                    help="config 2 scene: only the FP32 vs FP64 general-kernel leg (per-sample trajectory)")
     return ap.parse_args()
 
 
@@ -476,6 +478,28 @@ def run_general(sc, api, band, rows, pix, stream, bulk_gcorr):
             "vs_bulk": round(res["fp32"]["value"] / bulk_gcorr, 4)}
 
 
+def run_general_only(args):
+    """The general-kernel leg of the precision-study scene on its own (a JSON line)."""
+    import torch
+
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    torch.cuda.set_device(0)
+    sc = make_scene(args, "cuda")
+    api = sc.api_arrays()
+    rows = max(8, min(args.side, 64))
+    band = np.ascontiguousarray(sc.grid[:rows])
+    pix = sample_pixels(sc, 192)
+    build_oracle()
+    res = run_general(sc, api, band, rows, pix, torch.cuda.current_stream(), float("nan"))
+    res.pop("vs_bulk", None)
+    out = {"metric": "FP32 general kernel: Gcorr/s on per-sample trajectories", "unit": UNIT,
+           "value": res["value"], "higher_is_better": True, "dtype": "f32", "n_gpus": 1,
+           "config": {"workload": f"{rows} x {args.side} px band of the precision study, {sc.n_pri} chirps x "
+                                  f"{sc.n_samples} samples, FP32 positions drifting ~0.3 mm within each chirp"},
+           "general": res}
+    print(json.dumps(out), flush=True)
+
+
 def run_serving(args):
     """Config 4: a seeded Poisson stream of focus requests through the request loop, against
     the same jobs run one after another through the processor (FIFO, same arrival times)."""
@@ -706,6 +730,8 @@ def main():
         run_serving(args)
     elif args.config == "5":
         run_autofocus(args)
+    elif args.general_only:
+        run_general_only(args)
     else:
         run_ours(args)
     return 0
