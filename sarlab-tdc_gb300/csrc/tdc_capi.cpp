@@ -83,6 +83,8 @@ constexpr double kUniformPhaseTolRad = 1e-4;
 // FP32 general kernel: largest |(R_s^2 - R0^2) / R0^2| its range-change series takes, and
 // the bytes of chirp rows per pipeline stage it aims for.
 constexpr double kGeneralMaxEps = 0.1;
+constexpr double kGeneralNarrowEps = 0.02;
+constexpr double kGeneralNarrowCycles = 4.0;
 constexpr int kGeneralStageTarget = 32768;
 
 }  // namespace impl
@@ -455,13 +457,6 @@ int upload_grid(tdc_processor *p, int &launches)
     return TDC_OK;
 }
 
-int general_variant(const tdc_processor *p)
-{
-    const double rmax = max_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
-    const double dev = 2.0 * M_PI * 2.0 * p->resid_hz * rmax / kC0;
-    return (p->traj_varies ? 1 : 0) | (p->win_varies ? 2 : 0) | (dev > kUniformPhaseTolRad ? 4 : 0);
-}
-
 // Smallest distance between the antenna positions' bounding box and the grid's.
 double min_range(const double *amin, const double *amax, const double *gmin, const double *gmax)
 {
@@ -471,6 +466,31 @@ double min_range(const double *amin, const double *amax, const double *gmin, con
         r2 += d * d;
     }
     return std::sqrt(r2);
+}
+
+// Bound on |(R_s^2 - R0^2) / R0^2| over the acquisition (infinite when the antenna can
+// reach a pixel).
+double range_change_bound(const tdc_processor *p)
+{
+    const double rmin = min_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
+    if (!(rmin > 0.0)) return std::numeric_limits<double>::infinity();
+    const double q = p->delta_max / rmin;
+    return 2.0 * q + q * q;
+}
+
+int general_variant(const tdc_processor *p)
+{
+    const double rmax = max_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
+    const double dev = 2.0 * M_PI * 2.0 * p->resid_hz * rmax / kC0;
+    bool wide = dev > kUniformPhaseTolRad;
+    if (p->traj_varies) {
+        // the narrow variants take the range-change series to second order and the
+        // phase correction unreduced: |e| <= 0.02 and |g_s d_s| <= 4 cycles
+        const double g_max = 2.0 * (std::fabs(p->F0) + std::fabs(p->F1) * std::max(0, p->S - 1)) / kC0 +
+                             2.0 * p->resid_hz / kC0;
+        wide = wide || range_change_bound(p) > kGeneralNarrowEps || g_max * p->delta_max > kGeneralNarrowCycles;
+    }
+    return (p->traj_varies ? 1 : 0) | (p->win_varies ? 2 : 0) | (wide ? 4 : 0);
 }
 
 int choose_path(const tdc_processor *p)
@@ -487,14 +507,9 @@ int choose_path(const tdc_processor *p)
         return TDC_PATH_FP32_BULK;
     }
     if (fp64) return TDC_PATH_GENERAL_FP64;
-    if (variant & 1) {
-        // Per-sample range change d_s = N/(2 R0) f(N/R0^2): the series of f stays accurate for
-        // |N/R0^2| <= 2 dmax/Rmin + (dmax/Rmin)^2 <= 0.1.
-        const double rmin = min_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
-        if (!(rmin > 0.0)) return TDC_PATH_GENERAL_FP64;
-        const double q = p->delta_max / rmin;
-        if (2.0 * q + q * q > kGeneralMaxEps) return TDC_PATH_GENERAL_FP64;
-    }
+    // Per-sample range change d_s = N/(2 R0) f(N/R0^2): the series of f stays accurate for
+    // |N/R0^2| <= 2 dmax/Rmin + (dmax/Rmin)^2 <= 0.1.
+    if ((variant & 1) && !(range_change_bound(p) <= kGeneralMaxEps)) return TDC_PATH_GENERAL_FP64;
     int cb = 1;
     const int stage_bytes = general_stage_bytes_for(p->s_pad, variant, cb);
     // 227 KiB of shared memory per CTA, less the kernel's static shared memory

@@ -18,8 +18,11 @@
 // d_s comes without cancellation from the per-sample offset D_s = P[c,s] - P[c,0]:
 //   N = D.(2 (P0 - T) + D) = R_s^2 - R0^2,   d_s = N / (R0 + R_s) = (N / 2R0) f(N / R0^2),
 //   f(e) = 2 / (1 + sqrt(1 + e)) = 1 - e/4 + e^2/8 - 5e^3/64 + 7e^4/128 - ...,
-// the series taken to e^4 (the host routes |e| > 0.1 to the FP64 kernel; at 0.1 the
-// truncation is 4e-7 of d_s). psi_s is reduced modulo one cycle before the sincos.
+// the series taken to e^2 when the host bounds |e| <= 0.02 and |psi| <= 4 cycles (then
+// the sincos takes psi unreduced: its argument scaling adds < 2e-6 rad), else to e^4 with
+// psi reduced modulo one cycle ("wide" variants, which also carry the non-uniform
+// sampling residual; the host routes |e| > 0.1 to the FP64 kernel; at 0.1 the
+// truncation is 4e-7 of d_s).
 //
 // Same unit decomposition, staging (cp.async.bulk + mbarrier pipeline), skip test,
 // Kahan accumulation and FP64 group reduction as the bulk kernel.
@@ -33,9 +36,13 @@ namespace tdc {
 
 namespace {
 
+#ifndef TDC_GENERAL_MINB
+#define TDC_GENERAL_MINB 1
+#endif
+
 constexpr int kL = 8;                   // in-block phasor table length
-constexpr int kT = kFocusThreads;       // threads per CTA
 constexpr int kPT = kGeneralPT;         // pixels per thread
+constexpr int kT = kFocusTile / kPT;    // threads per CTA (a CTA covers one 512-pixel tile)
 constexpr int kTile = kT * kPT;
 // Double buffering: a chirp row takes tens of microseconds of arithmetic per CTA, far
 // longer than its copy, and the smaller footprint keeps two CTAs resident per SM.
@@ -58,8 +65,8 @@ __device__ __forceinline__ float round_small(float v)
     return (v + kMagic) - kMagic;
 }
 
-template <bool TRAJ, bool WIN, bool NONUNIF>
-__global__ void __launch_bounds__(kT, 1)
+template <bool TRAJ, bool WIN, bool WIDE>
+__global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
     focus_general_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                          int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
 {
@@ -145,7 +152,7 @@ __global__ void __launch_bounds__(kT, 1)
             sp.t[i * 6 + 4][tid] = lo.y;
             sp.t[i * 6 + 5][tid] = lo.z;
         }
-        if (NONUNIF) {
+        if (WIDE) {
             for (int s = tid; s < s_pad; s += kT) sres[s] = sJ.gres[s];
             __syncthreads();
         }
@@ -262,24 +269,31 @@ __global__ void __launch_bounds__(kT, 1)
                         float4 av = make_float4(0.f, 0.f, 0.f, 0.f), bv = av;
                         if (TRAJ) av = as[s];
                         if (WIN) bv = bs[s];
-                        const float res = NONUNIF ? sres[s] : 0.0f;
+                        const float res = WIDE ? sres[s] : 0.0f;
 #pragma unroll
                         for (int i = 0; i < kPT; ++i) {
                             float yr = xr, yi = xi;
-                            if (TRAJ || NONUNIF) {
+                            if (TRAJ || WIDE) {
                                 float psi = 0.0f;
                                 if (TRAJ) {
                                     const float nx = av.x + t2x[i], ny = av.y + t2y[i], nz = av.z + t2z[i];
                                     const float n = fmaf(av.x, nx, fmaf(av.y, ny, av.z * nz));
                                     const float e = n * b2[i];
-                                    float f = fmaf(e, 7.0f / 128.0f, -5.0f / 64.0f);
-                                    f = fmaf(f, e, 0.125f);
-                                    f = fmaf(f, e, -0.25f);
+                                    float f;
+                                    if (WIDE) {
+                                        f = fmaf(e, 7.0f / 128.0f, -5.0f / 64.0f);
+                                        f = fmaf(f, e, 0.125f);
+                                        f = fmaf(f, e, -0.25f);
+                                    } else {
+                                        f = fmaf(e, 0.125f, -0.25f);
+                                    }
                                     f = fmaf(f, e, 1.0f);
                                     psi = av.w * ((n * a2[i]) * f);  // g_s d_s
                                 }
-                                if (NONUNIF) psi = fmaf(res, r0[i], psi);
-                                psi -= round_small(psi);
+                                if (WIDE) {
+                                    psi = fmaf(res, r0[i], psi);
+                                    psi -= round_small(psi);
+                                }
                                 float sn, cs;
                                 __sincosf(kTwoPiF * psi, &sn, &cs);
                                 yr = fmaf(xr, cs, -xi * sn);
@@ -351,9 +365,9 @@ __global__ void __launch_bounds__(kT, 1)
     }
 }
 
-template <bool TRAJ, bool WIN, bool NONUNIF>
+template <bool TRAJ, bool WIN, bool WIDE>
 struct GeneralKernel {
-    static constexpr auto fn = focus_general_kernel<TRAJ, WIN, NONUNIF>;
+    static constexpr auto fn = focus_general_kernel<TRAJ, WIN, WIDE>;
 };
 
 using KernelFn = void (*)(const FocusJob *, const FocusUnit *, int, int *, int *, int);

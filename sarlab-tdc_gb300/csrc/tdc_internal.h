@@ -127,7 +127,8 @@ cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_d
 cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P, float2 *image,
                                 cudaStream_t st);
 // FP32 general focus (tdc_general.cu). variant bits: 1 per-sample positions, 2 per-sample
-// windows, 4 non-uniform sampling (at least one set).
+// windows, 4 wide (non-uniform sampling residual, large intra-chirp motion: reduced phase
+// correction, longer range-change series); at least one set.
 cudaError_t launch_focus_general(int variant, const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                                  int *counter_dev, int *status_dev, int stage_bytes, int s_pad, int grid_ctas,
                                  cudaStream_t st);

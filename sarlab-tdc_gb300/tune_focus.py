@@ -9,10 +9,18 @@ synthetic shapes with the acquisition and grid resident on the device:
     3: 1024^2 pixels x 4096 chirps x  256 samples (the 3-D volume's sample count)
     1: 256^2 pixels x 1024 chirps x 512 samples (the small stripmap case)
 
+and, for the general kernel (TDC_GENERAL_PT, TDC_GENERAL_MINB), on 512^2 pixels x
+1024 chirps x 1024 samples with FP32 per-sample inputs:
+
+    g:  positions drifting ~0.3 mm within each chirp
+    gw: the same plus per-sample velocity under a 30 Hz Doppler band
+    gn: jittered (non-uniform) sample times
+
 Timing: 2 warm-up focuses, then the mean of 3 focuses between CUDA events on the
 launching stream. Each variant's image is compared with the first variant's.
 
     python sarlab-tdc_gb300/tune_focus.py base= u4=-DTDC_FOCUS_UNROLL=4 "s4=-DTDC_FOCUS_SWAP=1 -DTDC_FOCUS_UNROLL=4"
+    python sarlab-tdc_gb300/tune_focus.py --shapes g,gw,gn base= "pt2=-DTDC_GENERAL_PT=2 -DTDC_GENERAL_MINB=2"
 """
 from __future__ import annotations
 
@@ -35,17 +43,39 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     import _sarlabtdc
     from sarlabtdc import scenes
 
+    band = float("inf")
     if shape == "1":
         sc = scenes.config1(device="cuda")
+    elif shape.startswith("g"):
+        sc = scenes.config2(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
     else:
         sc = scenes.config2(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=1024 if shape == "2" else 256,
                             n_targets=8)
     api = sc.api_arrays()
     p = _sarlabtdc.TdcProcessor(0)
-    p.setRawData(*api.values())
-    p.setChirpPositionsF64(sc.positions)
-    p.setFocusGridF64(sc.grid)
-    p.prepare(0.0, float("inf"), False, False, True)
+    if shape.startswith("g"):
+        C, S = sc.n_pri, sc.n_samples
+        rng = np.random.default_rng(1)
+        if shape in ("g", "gw"):
+            pos = np.broadcast_to(sc.positions[:, None, :], (C, S, 3)) + \
+                (np.arange(S) / S)[None, :, None] * rng.normal(0.0, 0.3e-3, (C, 1, 3))
+            api["position"] = np.ascontiguousarray(pos, dtype=np.float32)
+        if shape == "gw":
+            vel = np.zeros((C, S, 3), np.float32)
+            vel[..., 0] = 0.05 + 0.01 * np.sin(np.arange(S) / 7.0)[None, :]
+            api["velocity"] = vel
+            band = 30.0
+        if shape == "gn":
+            st = api["sampleTimes"].astype(np.float64)
+            st += rng.uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
+            api["sampleTimes"] = st.astype(np.float32)
+        p.setRawData(*api.values())
+        p.setFocusGrid(sc.grid.astype(np.float32))
+    else:
+        p.setRawData(*api.values())
+        p.setChirpPositionsF64(sc.positions)
+        p.setFocusGridF64(sc.grid)
+    p.prepare(0.0, band, False, False, True)
     p.uploadGrid()
     img = torch.empty(p.numPixels(), dtype=torch.complex64, device="cuda")
     for _ in range(2):
@@ -65,7 +95,7 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     if not ref_f.exists():
         np.save(ref_f, out)
     ref = np.load(ref_f)
-    return {"ms": round(ms, 3), "gcorr_s": round(sc.correlations() / (ms / 1e3) / 1e9, 1),
+    return {"ms": round(ms, 3), "gcorr_s": round(sc.correlations() / (ms / 1e3) / 1e9, 1), "path": p.path(),
             "rel_vs_first": float(np.linalg.norm(out - ref) / np.linalg.norm(ref))}
 
 
@@ -76,12 +106,16 @@ def main(argv: list[str]) -> int:
     sys.path.insert(0, str(PKG))
     import build as engine_build
 
+    shapes = SHAPES
+    if argv[:1] == ["--shapes"]:
+        shapes = tuple(argv[1].split(","))
+        argv = argv[2:]
     variants = [a.split("=", 1) for a in argv] or [["base", ""]]
     ref_dir = Path(tempfile.mkdtemp(prefix="tdc_tune_"))
     for name, flags in variants:
         out_dir = engine_build.BUILD / "variants" / name
         lib = engine_build.build(defines=tuple(flags.split()), out_dir=out_dir, lib=out_dir / "libtdc_gb300.so")
-        for shape in SHAPES:
+        for shape in shapes:
             r = subprocess.run([sys.executable, __file__, "--time", shape, str(ref_dir)],
                                env={**os.environ, "TDC_GB300_LIB": str(lib)}, capture_output=True, text=True,
                                timeout=900)

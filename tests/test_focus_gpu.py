@@ -362,15 +362,16 @@ def _general_api(sc, traj=False, win=False, nonunif=False, drift=0.3e-3, seed=5)
     return api
 
 
-@pytest.mark.parametrize("case", ["traj", "win", "traj_win", "nonunif", "traj_nonunif", "all"])
+@pytest.mark.parametrize("case", ["traj", "traj_wide", "win", "traj_win", "nonunif", "traj_nonunif", "all"])
 def test_fp32_general_kernel_variants(cuda_device, case):
     """FP32 general kernel (per-sample positions / windows, non-uniform sampling) against the
-    FP64 oracle, which evaluates range, phase and window per element."""
+    FP64 oracle, which evaluates range, phase and window per element. traj_wide moves the
+    antenna centimetres within a chirp (the longer range-change series, reduced phase)."""
     sc = scenes.small_scene(seed=31, n_pri=200, n_samples=80, nx=17, ny=13, device="cuda")
     traj = "traj" in case or case == "all"
     win = "win" in case or case == "all"
     nonunif = "nonunif" in case or case == "all"
-    api = _general_api(sc, traj=traj, win=win, nonunif=nonunif)
+    api = _general_api(sc, traj=traj, win=win, nonunif=nonunif, drift=3e-3 if case == "traj_wide" else 0.3e-3)
     args = (0.0, 30.0 if win else INF, False, True, True)
     img, stats, _ = run_engine(api, sc.grid, args)
     assert stats["path_name"] == "general"
