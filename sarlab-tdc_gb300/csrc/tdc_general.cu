@@ -37,7 +37,7 @@ namespace tdc {
 namespace {
 
 #ifndef TDC_GENERAL_MINB
-#define TDC_GENERAL_MINB 1
+#define TDC_GENERAL_MINB 2
 #endif
 
 constexpr int kL = 8;                   // in-block phasor table length

@@ -30,7 +30,7 @@ constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows
 constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp rows + records per pipeline stage
 // Pixels per thread of the FP32 general kernel (per-sample trajectories / windows, non-uniform sampling).
 #ifndef TDC_GENERAL_PT
-#define TDC_GENERAL_PT 4
+#define TDC_GENERAL_PT 2
 #endif
 constexpr int kGeneralPT = TDC_GENERAL_PT;
 
