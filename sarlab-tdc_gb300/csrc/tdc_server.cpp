@@ -145,6 +145,7 @@ struct tdc_server {
     // Launches alternate between two streams, so the next launch's CTAs take the
     // SMs that the previous launch's last units leave idle.
     cudaStream_t compute[2] = {nullptr, nullptr};
+    cudaStream_t side = nullptr;  // unbatched jobs (FP64 / general paths), launch priority
     Batch batches[2];
     int next_batch = 0;
     tdc_server_stats stats{};
@@ -464,14 +465,15 @@ void tdc_server::admit_loop()
         int rc2 = TDC_OK;
         std::string err2;
         if (!rc && j->plan.path != TDC_PATH_FP32_BULK) {
-            // FP64 / general path: not batched, focused on its own on the slot's stream.
+            // FP64 / general path: not batched, focused on its own on the side stream (at the
+            // launch streams' priority, so it shares the SMs with the batches).
             tdc_processor *p = j->slot;
-            rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), p->stream);
+            rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), side);
             if (rc2) {
                 err2 = tdc_last_error();
             } else if (cudaMemcpyAsync(p->image_host.p, p->image_dev.p, (size_t)p->P * 8, cudaMemcpyDeviceToHost,
-                                       p->stream) != cudaSuccess ||
-                       cudaEventRecord(j->done_ev, p->stream) != cudaSuccess) {
+                                       side) != cudaSuccess ||
+                       cudaEventRecord(j->done_ev, side) != cudaSuccess) {
                 rc2 = TDC_ERR_CUDA;
                 err2 = "image copy";
             }
@@ -553,6 +555,8 @@ int tdc_server_create(int device, size_t memory_budget_bytes, int max_jobs, tdc_
         if (cudaStreamCreateWithPriority(&s->compute[i], cudaStreamNonBlocking, least) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->batches[i].ev, cudaEventDisableTiming) != cudaSuccess)
             rc = set_last_error(TDC_ERR_CUDA, "stream / event creation failed");
+    if (!rc && cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, least) != cudaSuccess)
+        rc = set_last_error(TDC_ERR_CUDA, "stream creation failed");
     for (int i = 0; i < s->max_jobs && !rc; ++i) {
         tdc_processor *p = nullptr;
         rc = tdc_processor_create(device, &p);
@@ -653,7 +657,7 @@ int tdc_server_destroy(tdc_server *s)
     if (s->th_admit.joinable()) s->th_admit.join();
     if (s->th_launch.joinable()) s->th_launch.join();
     cudaSetDevice(s->device);
-    for (cudaStream_t st : s->compute)
+    for (cudaStream_t st : {s->compute[0], s->compute[1], s->side})
         if (st) cudaStreamSynchronize(st);
     for (auto &kv : s->jobs)
         if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
@@ -663,7 +667,7 @@ int tdc_server_destroy(tdc_server *s)
         b.host.release();
     }
     for (tdc_processor *p : s->slots) tdc_processor_destroy(p);
-    for (cudaStream_t st : s->compute)
+    for (cudaStream_t st : {s->compute[0], s->compute[1], s->side})
         if (st) cudaStreamDestroy(st);
     delete s;
     return TDC_OK;

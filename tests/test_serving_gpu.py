@@ -106,3 +106,33 @@ def test_job_over_budget_fails_alone(cuda_device):
             srv.wait(bid)
         img, info = srv.wait(sid)
         assert info["status"] == 0
+
+
+def test_unbatched_general_path_job_in_a_mix(cuda_device):
+    """A job the FP32-bulk kernel cannot take (jittered sample times: FP32 general kernel) runs
+    unbatched beside batched jobs and gives the processor's image bit for bit."""
+    import _sarlabtdc
+    from sarlabtdc.serving import FocusServer
+
+    jobs = _jobs()[:3]
+    odd = scenes.small_scene(seed=13, n_pri=300, n_samples=96, nx=40, ny=30, jitter=0.2e-3, device="cuda")
+    st = odd.radar.sample_times().astype(np.float64)
+    st += np.random.default_rng(4).uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
+    st = st.astype(np.float32)
+    with FocusServer(max_jobs=4) as srv:
+        ids = [_submit(srv, sc) for sc in jobs]
+        oid = srv.submit(odd.raw, st, odd.positions, odd.grid, np.float32(odd.radar.mod_rate),
+                         np.float32(odd.radar.f0), start=START)
+        img, info = srv.wait(oid)
+        for i in ids:
+            assert srv.wait(i)[1]["status"] == 0
+    assert info["status"] == 0 and info["path"] == 2
+    p = _sarlabtdc.TdcProcessor(0)
+    api = odd.api_arrays()
+    api["sampleTimes"] = st
+    p.setRawData(*api.values())
+    p.setChirpPositionsF64(odd.positions)
+    p.setFocusGridF64(odd.grid)
+    p.start(*START)
+    assert p.lastStats()["path_name"] == "general"
+    np.testing.assert_array_equal(p.getFocusedImage().ravel(), img)
