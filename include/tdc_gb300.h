@@ -303,6 +303,13 @@ int tdc_server_destroy(tdc_server *srv);
  * in practice). */
 int tdc_probe_fma(int fp64, int blocks, int iters, void *scratch_dev, double *flops, void *stream);
 
+/* Self-test of the kernels' failure detection: one CTA waits, with the same bounded
+ * mbarrier wait the focus kernels use, on a barrier phase that nothing completes. After
+ * limit_us (at most 2 s) the wait gives up, the CTA sets the timeout bit of a status word
+ * and returns; *timed_out receives that bit (1 expected), *elapsed_ms (optional) the
+ * kernel's duration. The device stays usable afterwards. */
+int tdc_selftest_wait_timeout(int device, int limit_us, int *timed_out, double *elapsed_ms);
+
 /* ---- focus without allocation (no counterpart in the reference) ---- */
 
 /*

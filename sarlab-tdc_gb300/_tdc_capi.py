@@ -158,6 +158,7 @@ SIGNATURES = [
     ("tdc_processor_reads_host_memory", C.c_int, [_vp]),
     ("tdc_processor_set_image_output", C.c_int, [_vp, _vp, C.c_int64]),
     ("tdc_probe_fma", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.POINTER(C.c_double), _vp]),
+    ("tdc_selftest_wait_timeout", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("tdc_focus_noalloc", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp]),
     ("tdc_processor_set_chirp_offsets_device", C.c_int, [_vp, _vp, _vp]),
     ("tdc_processor_adjoint_device", C.c_int, [_vp, _vp, _vp, _vp]),

@@ -159,3 +159,15 @@ def _cpp_build(tmp_path):
 def test_cpp_header_compiles_and_links(engine_lib, tmp_path):
     """include/tdcprocessor.h is a drop-in for the reference's class: a tdctest-shaped program builds."""
     assert _cpp_build(tmp_path).exists()
+
+
+def test_wait_timeout_selftest_rejects_bad_limits_before_any_cuda_call(engine_lib):
+    import ctypes as C
+
+    import _tdc_capi
+
+    flag = C.c_int(7)
+    for limit in (0, -5, 3_000_000):
+        assert engine_lib.tdc_selftest_wait_timeout(0, limit, C.byref(flag), None) == _tdc_capi.TDC_ERR_INVALID_ARGUMENT
+    assert engine_lib.tdc_selftest_wait_timeout(0, 1000, None, None) == _tdc_capi.TDC_ERR_INVALID_ARGUMENT
+    assert flag.value == 7
