@@ -106,6 +106,14 @@ def skip_nonzero(pos_st, vel_st, att_st, S, tgt, bore, lam, center, bw, centroid
     return m <= float(np.float32(bw)) / 2.0
 
 
+def per_sample(a, n_pri, n_samples):
+    """[C, k] per-chirp rows broadcast to the reference's [C, S, k], or [C, S, k] as given."""
+    a = np.asarray(a, np.float32)
+    if a.ndim == 2:
+        a = np.broadcast_to(a[:, None, :], (n_pri, n_samples, a.shape[1]))
+    return np.ascontiguousarray(a)
+
+
 def reference_focus(drv, case):
     import torch
 
@@ -113,9 +121,7 @@ def reference_focus(drv, case):
 
     raw, st = case["raw"], case["sample_times"]
     C_, S = raw.shape
-    pos = np.ascontiguousarray(np.broadcast_to(case["pos"][:, None, :], (C_, S, 3)), np.float32)
-    vel = np.ascontiguousarray(np.broadcast_to(case["vel"][:, None, :], (C_, S, 3)), np.float32)
-    att = np.ascontiguousarray(np.broadcast_to(case["att"][:, None, :], (C_, S, 4)), np.float32)
+    pos, vel, att = (per_sample(case[k], C_, S) for k in ("pos", "vel", "att"))
     grid = case["grid"].reshape(-1, 3).astype(np.float32)
     K, f0 = float(np.float32(case["mod_rate"])), float(np.float32(case["start_freq"]))
     center, bw = float(case["center"]), float(case["bw"])
@@ -198,6 +204,34 @@ def make_cases():
                          grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
                          start_freq=np.float32(sc.radar.f0), center=1.0, bw=24.0, centroid=0, apply_range_win=0,
                          taper=0, bore=np.array([0, 1, 0], np.float32))
+    # D: per-sample trajectory: the antenna keeps moving within each chirp (positions drift
+    # up to ~0.5 mm per chirp), per-sample velocity, centroid window with taper, skip test,
+    # 200 PRIs (a partial last chunk)
+    rng = np.random.default_rng(105)
+    sc = scenes.small_scene(seed=106, n_pri=200, n_samples=48, nx=10, ny=9, rail_len=0.3, device="cuda")
+    C_, S = 200, 48
+    frac = (np.arange(S) / S)[None, :, None]
+    pos = sc.positions[:, None, :] + frac * rng.normal(0.0, 0.3e-3, (C_, 1, 3))
+    vel = np.zeros((C_, S, 3))
+    vel[..., 0] = 0.05 + 0.01 * np.sin(np.arange(S) / 5.0)[None, :]
+    vel[..., 1] = rng.normal(0.0, 0.01, (C_, 1))
+    yaw = rng.normal(0, 0.02, C_)
+    att = np.stack([np.cos(yaw / 2), 0 * yaw, 0 * yaw, np.sin(yaw / 2)], 1)
+    cases["persample"] = dict(raw=sc.raw, sample_times=sc.radar.sample_times(), pos=pos.astype(np.float32),
+                              vel=vel.astype(np.float32), att=per_sample(att, C_, S),
+                              grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
+                              start_freq=np.float32(sc.radar.f0), center=2.0, bw=20.0, centroid=1,
+                              apply_range_win=1, taper=1, bore=np.array([0, 1, 0], np.float32))
+    # E: non-uniform (jittered) sample times, infinite Doppler band
+    sc = scenes.small_scene(seed=107, n_pri=160, n_samples=56, nx=10, ny=8, jitter=0.2e-3, device="cuda")
+    st = sc.radar.sample_times().astype(np.float64)
+    st += np.random.default_rng(108).uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
+    cases["nonuniform"] = dict(raw=sc.raw, sample_times=st.astype(np.float32), pos=sc.positions.astype(np.float32),
+                               vel=np.zeros((160, 3), np.float32),
+                               att=np.tile([1, 0, 0, 0], (160, 1)).astype(np.float32),
+                               grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
+                               start_freq=np.float32(sc.radar.f0), center=0.0, bw=float("inf"), centroid=0,
+                               apply_range_win=1, taper=1, bore=np.array([0, 1, 0], np.float32))
     return cases
 
 

@@ -1,6 +1,6 @@
 """Parity against the reference's own GPU output.
 
-tests/golden/ref_gpu_images.npz holds three small acquisitions and the images
+tests/golden/ref_gpu_images.npz holds five small acquisitions and the images
 the reference's kernels (tdc-lib/src/tdckernels.cu, compiled from its source to
 PTX and launched in the order of tdcprocessor.cpp:59-167) produced for them on a
 GB300; tests/golden/make_ref_gpu_golden.py made it. The oracle (CPU) and the
@@ -37,19 +37,27 @@ def _opts(c):
                        dopplerWinTaper=bool(c["taper"]))
 
 
+def _per_sample(a, n_pri, n_samples):
+    a = np.asarray(a, np.float32)
+    if a.ndim == 2:
+        a = np.broadcast_to(a[:, None, :], (n_pri, n_samples, a.shape[1]))
+    return np.ascontiguousarray(a)
+
+
 def _api(c):
     raw = c["raw"]
     C_, S = raw.shape
-    b = lambda a, k: np.ascontiguousarray(np.broadcast_to(a.astype(np.float32)[:, None, :], (C_, S, k)))
     return dict(rawData=raw, priTimes=np.zeros(C_, np.float32), sampleTimes=c["sample_times"],
-                position=b(c["pos"], 3), velocity=b(c["vel"], 3), attitude=b(c["att"], 4),
-                modRate=c["mod_rate"], startFreq=c["start_freq"], bodyBoresight=c["bore"])
+                position=_per_sample(c["pos"], C_, S), velocity=_per_sample(c["vel"], C_, S),
+                attitude=_per_sample(c["att"], C_, S), modRate=c["mod_rate"], startFreq=c["start_freq"],
+                bodyBoresight=c["bore"])
 
 
 def test_oracle_matches_reference_gpu_images():
     for name, c in _cases().items():
-        prob = oracle.Problem(raw=c["raw"], sampleTimes=c["sample_times"], position=c["pos"].astype(np.float64),
-                              velocity=c["vel"].astype(np.float64), attitude=c["att"].astype(np.float64),
+        api = _api(c)
+        prob = oracle.Problem(raw=c["raw"], sampleTimes=c["sample_times"], position=api["position"],
+                              velocity=api["velocity"], attitude=api["attitude"],
                               modRate=c["mod_rate"], startFreq=c["start_freq"], grid=c["grid"],
                               bodyBoresight=tuple(c["bore"]))
         img = oracle.focus(prob, _opts(c))
@@ -67,6 +75,8 @@ def test_engine_matches_reference_gpu_images(cuda_device):
         api = _api(c)
         args = (float(c["center"]), float(c["bw"]), bool(c["centroid"]), bool(c["apply_range_win"]),
                 bool(c["taper"]))
-        img, _, _ = run_engine(api, c["grid"], args)
+        img, stats, _ = run_engine(api, c["grid"], args)
         err = rel_l2(img.ravel(), c["image"])
         assert err <= TOL, f"{name}: engine vs reference GPU image, relative L2 {err:.2e}"
+        if c["pos"].ndim == 3 or name == "nonuniform":
+            assert stats["path_name"] == "general", name
