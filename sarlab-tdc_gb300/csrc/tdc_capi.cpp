@@ -11,6 +11,7 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tdc_gb300.h"
@@ -153,6 +154,26 @@ double max_range(const double *amin, const double *amax, const double *gmin, con
 
 void stats_reset(tdc_processor *p) { std::memset(&p->stats, 0, sizeof(p->stats)); }
 
+// fn(thread, begin, end) over chirps [0, n) on up to 16 host threads, about 1M elements
+// (chirps x per_item) or more per thread; returns the number of threads used.
+template <class F>
+int parallel_chirps(int n, long long per_item, F fn)
+{
+    const long long total = (long long)n * std::max(1LL, per_item);
+    const long long hw = std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+    const int nt = (int)std::max(1LL, std::min({hw, total >> 20, (long long)n}));
+    if (nt <= 1) {
+        fn(0, 0, n);
+        return 1;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back(fn, t, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+    for (std::thread &th : pool) th.join();
+    return nt;
+}
+
 // Upload + prepare the acquisition for the given start() options.
 int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 {
@@ -204,10 +225,23 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         }
     }
     if (!p->per_chirp && p->pos && !p->pos64) {
-        for (size_t i = 0; i < (size_t)C * S; ++i)
+        std::vector<double> box(16 * 6);
+        const int nt = parallel_chirps(C, S, [&](int t, int c0, int c1) {
+            double *b = &box[6 * t];
             for (int k = 0; k < 3; ++k) {
-                p->ant_min[k] = std::min(p->ant_min[k], (double)p->pos[3 * i + k]);
-                p->ant_max[k] = std::max(p->ant_max[k], (double)p->pos[3 * i + k]);
+                b[k] = std::numeric_limits<double>::infinity();
+                b[3 + k] = -std::numeric_limits<double>::infinity();
+            }
+            for (size_t i = (size_t)c0 * S; i < (size_t)c1 * S; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    b[k] = std::min(b[k], (double)p->pos[3 * i + k]);
+                    b[3 + k] = std::max(b[3 + k], (double)p->pos[3 * i + k]);
+                }
+        });
+        for (int t = 0; t < nt; ++t)
+            for (int k = 0; k < 3; ++k) {
+                p->ant_min[k] = std::min(p->ant_min[k], box[6 * t + k]);
+                p->ant_max[k] = std::max(p->ant_max[k], box[6 * t + 3 + k]);
             }
     }
 
@@ -216,30 +250,32 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     static const float kQId[4] = {1.f, 0.f, 0.f, 0.f};
     const size_t n_rec = p->per_chirp ? (size_t)C : (size_t)C * S;
     std::vector<ChirpRec> recs(n_rec);
-    for (int c = 0; c < C; ++c) {
-        const int ns = p->per_chirp ? 1 : S;
-        for (int s = 0; s < ns; ++s) {
-            const size_t e = (size_t)c * S + s;
-            const size_t te = ti(c, s);
-            const float *vl = p->vel ? p->vel + 3 * te : kZero3;
-            const float *at = p->att ? p->att + 4 * te : kQId;
-            const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
-            ChirpRec r;
-            float h[3], l[3];
-            for (int k = 0; k < 3; ++k) {
-                if (p->pos64) {
-                    split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
-                } else {
-                    h[k] = p->pos[3 * te + k];
-                    l[k] = 0.f;
+    parallel_chirps(C, p->per_chirp ? 1 : S, [&](int, int cb, int ce) {
+        for (int c = cb; c < ce; ++c) {
+            const int ns = p->per_chirp ? 1 : S;
+            for (int s = 0; s < ns; ++s) {
+                const size_t e = (size_t)c * S + s;
+                const size_t te = ti(c, s);
+                const float *vl = p->vel ? p->vel + 3 * te : kZero3;
+                const float *at = p->att ? p->att + 4 * te : kQId;
+                const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
+                ChirpRec r;
+                float h[3], l[3];
+                for (int k = 0; k < 3; ++k) {
+                    if (p->pos64) {
+                        split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
+                    } else {
+                        h[k] = p->pos[3 * te + k];
+                        l[k] = 0.f;
+                    }
                 }
+                r.p_hi = make_float4(h[0], h[1], h[2], fdc);
+                r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
+                r.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
+                recs[p->per_chirp ? (size_t)c : e] = r;
             }
-            r.p_hi = make_float4(h[0], h[1], h[2], fdc);
-            r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
-            r.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
-            recs[p->per_chirp ? (size_t)c : e] = r;
         }
-    }
+    });
 
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
     const int s_pad = (int)round_up((size_t)S, kSampleAlign);
@@ -257,34 +293,43 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     if (!p->per_chirp) {
         rec0.resize(C);
         for (int c = 0; c < C; ++c) rec0[c] = recs[(size_t)c * S];
-        for (size_t i = 0; i < (size_t)C * S && p->vel && !any_velocity; ++i)
-            any_velocity = p->vel[3 * i] != 0.f || p->vel[3 * i + 1] != 0.f || p->vel[3 * i + 2] != 0.f;
+        for (int c = 0; c < C && !any_velocity; ++c) {
+            const ChirpRec *r = &recs[(size_t)c * S];
+            for (int s = 0; s < S && !any_velocity; ++s)
+                any_velocity = r[s].vel.x != 0.f || r[s].vel.y != 0.f || r[s].vel.z != 0.f;
+        }
     }
     // The window can change within a chirp when the band is finite and either the motion
     // varies per sample or a moving antenna's direction to the pixel does.
     p->win_varies = !p->per_chirp && std::isfinite(o.bw) && (motion_differ || (pos_differ && any_velocity));
     if (p->traj_varies) {
         traj.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
-        double d2max = 0.0;
-        for (int c = 0; c < C; ++c) {
-            const float *p0 = p->pos + 3 * ti(c, 0);
-            for (int s = 0; s < S; ++s) {
-                const float *ps = p->pos + 3 * ti(c, s);
-                const double dx = (double)ps[0] - p0[0], dy = (double)ps[1] - p0[1], dz = (double)ps[2] - p0[2];
-                d2max = std::max(d2max, dx * dx + dy * dy + dz * dz);
-                const double gsv = g0 + g1 * s + (double)gres[s];
-                traj[(size_t)c * s_pad + s] = make_float4((float)dx, (float)dy, (float)dz, (float)gsv);
+        std::vector<double> d2(16, 0.0);
+        const int nt = parallel_chirps(C, S, [&](int t, int cb, int ce) {
+            double m = 0.0;
+            for (int c = cb; c < ce; ++c) {
+                const float *p0 = p->pos + 3 * ti(c, 0);
+                for (int s = 0; s < S; ++s) {
+                    const float *ps = p->pos + 3 * ti(c, s);
+                    const double dx = (double)ps[0] - p0[0], dy = (double)ps[1] - p0[1], dz = (double)ps[2] - p0[2];
+                    m = std::max(m, dx * dx + dy * dy + dz * dz);
+                    const double gsv = g0 + g1 * s + (double)gres[s];
+                    traj[(size_t)c * s_pad + s] = make_float4((float)dx, (float)dy, (float)dz, (float)gsv);
+                }
             }
-        }
-        p->delta_max = std::sqrt(d2max);
+            d2[t] = m;
+        });
+        p->delta_max = std::sqrt(*std::max_element(d2.begin(), d2.begin() + nt));
     }
     if (p->win_varies) {
         wins.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
-        for (int c = 0; c < C; ++c)
-            for (int s = 0; s < S; ++s) {
-                const ChirpRec &r = recs[(size_t)c * S + s];
-                wins[(size_t)c * s_pad + s] = make_float4(r.vel.x, r.vel.y, r.vel.z, r.p_hi.w);
-            }
+        parallel_chirps(C, S, [&](int, int cb, int ce) {
+            for (int c = cb; c < ce; ++c)
+                for (int s = 0; s < S; ++s) {
+                    const ChirpRec &r = recs[(size_t)c * S + s];
+                    wins[(size_t)c * s_pad + s] = make_float4(r.vel.x, r.vel.y, r.vel.z, r.p_hi.w);
+                }
+        });
     }
 
     // ---- skip-test points (tdcprocessor.cpp:347-383, stale staging rows included) ----
