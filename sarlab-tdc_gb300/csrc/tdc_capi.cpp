@@ -174,6 +174,33 @@ int parallel_chirps(int n, long long per_item, F fn)
     return nt;
 }
 
+const float kZero3[3] = {0.f, 0.f, 0.f};
+const float kQId[4] = {1.f, 0.f, 0.f, 0.f};
+
+// Trajectory record of (chirp c, sample s): position (double-float when FP64 positions
+// are set), window centre, velocity.
+ChirpRec make_record(const tdc_processor *p, int c, int s, bool centroid, float center)
+{
+    const size_t te = p->traj_per_chirp ? (size_t)c : (size_t)c * p->S + s;
+    const float *vl = p->vel ? p->vel + 3 * te : kZero3;
+    const float *at = p->att ? p->att + 4 * te : kQId;
+    const float fdc = window_centre(vl, at, p->bore, p->lambda, centroid, center);
+    float h[3], l[3];
+    for (int k = 0; k < 3; ++k) {
+        if (p->pos64) {
+            split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
+        } else {
+            h[k] = p->pos[3 * te + k];
+            l[k] = 0.f;
+        }
+    }
+    ChirpRec r;
+    r.p_hi = make_float4(h[0], h[1], h[2], fdc);
+    r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
+    r.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
+    return r;
+}
+
 // Upload + prepare the acquisition for the given start() options.
 int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 {
@@ -245,37 +272,14 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
             }
     }
 
-    // ---- trajectory records (per chirp, or per sample for the general path) ----
-    static const float kZero3[3] = {0.f, 0.f, 0.f};
-    static const float kQId[4] = {1.f, 0.f, 0.f, 0.f};
-    const size_t n_rec = p->per_chirp ? (size_t)C : (size_t)C * S;
-    std::vector<ChirpRec> recs(n_rec);
-    parallel_chirps(C, p->per_chirp ? 1 : S, [&](int, int cb, int ce) {
-        for (int c = cb; c < ce; ++c) {
-            const int ns = p->per_chirp ? 1 : S;
-            for (int s = 0; s < ns; ++s) {
-                const size_t e = (size_t)c * S + s;
-                const size_t te = ti(c, s);
-                const float *vl = p->vel ? p->vel + 3 * te : kZero3;
-                const float *at = p->att ? p->att + 4 * te : kQId;
-                const float fdc = window_centre(vl, at, p->bore, p->lambda, o.centroid != 0, o.center);
-                ChirpRec r;
-                float h[3], l[3];
-                for (int k = 0; k < 3; ++k) {
-                    if (p->pos64) {
-                        split_dd(p->pos64[3 * (size_t)c + k], h[k], l[k]);
-                    } else {
-                        h[k] = p->pos[3 * te + k];
-                        l[k] = 0.f;
-                    }
-                }
-                r.p_hi = make_float4(h[0], h[1], h[2], fdc);
-                r.p_lo = make_float4(l[0], l[1], l[2], 0.f);
-                r.vel = make_float4(vl[0], vl[1], vl[2], 0.f);
-                recs[p->per_chirp ? (size_t)c : e] = r;
-            }
-        }
+    // ---- trajectory records: one per chirp (the record of sample 0 when the trajectory
+    // varies within chirps; the FP64 general kernel's per-sample records are built only
+    // when that kernel runs, see sample_records) ----
+    std::vector<ChirpRec> recs(C);
+    parallel_chirps(C, 1, [&](int, int cb, int ce) {
+        for (int c = cb; c < ce; ++c) recs[c] = make_record(p, c, 0, o.centroid != 0, o.center);
     });
+    p->sample_recs_ready = false;
 
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
     const int s_pad = (int)round_up((size_t)S, kSampleAlign);
@@ -285,19 +289,13 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         const double gsv = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
         gres[s] = (float)(gsv - (g0 + g1 * s));
     }
-    std::vector<ChirpRec> rec0;
     std::vector<float4> traj, wins;
     p->traj_varies = pos_differ;
     p->delta_max = 0.0;
     bool any_velocity = false;
-    if (!p->per_chirp) {
-        rec0.resize(C);
-        for (int c = 0; c < C; ++c) rec0[c] = recs[(size_t)c * S];
-        for (int c = 0; c < C && !any_velocity; ++c) {
-            const ChirpRec *r = &recs[(size_t)c * S];
-            for (int s = 0; s < S && !any_velocity; ++s)
-                any_velocity = r[s].vel.x != 0.f || r[s].vel.y != 0.f || r[s].vel.z != 0.f;
-        }
+    if (!p->per_chirp && p->vel) {
+        const size_t n = (size_t)C * (p->traj_per_chirp ? 1 : S) * 3;
+        for (size_t i = 0; i < n && !any_velocity; ++i) any_velocity = p->vel[i] != 0.f;
     }
     // The window can change within a chirp when the band is finite and either the motion
     // varies per sample or a moving antenna's direction to the pixel does.
@@ -326,7 +324,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         parallel_chirps(C, S, [&](int, int cb, int ce) {
             for (int c = cb; c < ce; ++c)
                 for (int s = 0; s < S; ++s) {
-                    const ChirpRec &r = recs[(size_t)c * S + s];
+                    const ChirpRec r = make_record(p, c, s, o.centroid != 0, o.center);
                     wins[(size_t)c * s_pad + s] = make_float4(r.vel.x, r.vel.y, r.vel.z, r.p_hi.w);
                 }
         });
@@ -382,7 +380,10 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     cudaStream_t st = p->stream;
     TDC_CK(p->xw.ensure((size_t)C * s_pad * 8), "alloc samples");
     TDC_CK(p->wr.ensure((size_t)S * 4), "alloc range window");
-    TDC_CK(p->chirps.ensure(n_rec * sizeof(ChirpRec)), "alloc chirp records");
+    // sample-0 records go to gen_rec when the trajectory varies within chirps (chirps then
+    // holds the per-sample records of the FP64 general kernel, built on demand)
+    DevBuf &rec_buf = p->per_chirp ? p->chirps : p->gen_rec;
+    TDC_CK(rec_buf.ensure((size_t)C * sizeof(ChirpRec)), "alloc chirp records");
     TDC_CK(p->skip.ensure(skip.size() * sizeof(SkipPoint)), "alloc skip table");
     TDC_CK(p->gs.ensure((size_t)S * 8), "alloc frequency table");
     TDC_CK(p->pos_base.ensure((size_t)C * 3 * 8), "alloc base positions");
@@ -392,7 +393,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                                  cudaMemcpyHostToDevice, st),
                "copy raw data");
     }
-    TDC_CK(cudaMemcpyAsync(p->chirps.p, recs.data(), n_rec * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
+    TDC_CK(cudaMemcpyAsync(rec_buf.p, recs.data(), (size_t)C * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
            "copy chirp records");
     TDC_CK(cudaMemcpyAsync(p->skip.p, skip.data(), skip.size() * sizeof(SkipPoint), cudaMemcpyHostToDevice, st),
            "copy skip table");
@@ -402,11 +403,6 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(p->gres.ensure((size_t)s_pad * 4), "alloc residual frequency table");
     TDC_CK(cudaMemcpyAsync(p->gres.p, gres.data(), (size_t)s_pad * 4, cudaMemcpyHostToDevice, st),
            "copy residual frequency table");
-    if (!rec0.empty()) {
-        TDC_CK(p->gen_rec.ensure(rec0.size() * sizeof(ChirpRec)), "alloc sample-0 records");
-        TDC_CK(cudaMemcpyAsync(p->gen_rec.p, rec0.data(), rec0.size() * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
-               "copy sample-0 records");
-    }
     if (!traj.empty()) {
         TDC_CK(p->traj.ensure(traj.size() * sizeof(float4)), "alloc per-sample offsets");
         TDC_CK(cudaMemcpyAsync(p->traj.p, traj.data(), traj.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
@@ -417,9 +413,8 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         TDC_CK(cudaMemcpyAsync(p->wins.p, wins.data(), wins.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
                "copy per-sample windows");
     }
-    p->stats.h2d_bytes += (int64_t)s_pad * 4 + (int64_t)(rec0.size() * sizeof(ChirpRec)) +
-                          (int64_t)((traj.size() + wins.size()) * sizeof(float4));
-    p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)n_rec * sizeof(ChirpRec) +
+    p->stats.h2d_bytes += (int64_t)s_pad * 4 + (int64_t)((traj.size() + wins.size()) * sizeof(float4));
+    p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)C * sizeof(ChirpRec) +
                           (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
 
@@ -653,6 +648,28 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     return job;
 }
 
+// Per-(chirp, sample) records of the FP64 general kernel, built from the caller's
+// per-sample arrays the first time that kernel runs on the resident acquisition.
+int sample_records(tdc_processor *p)
+{
+    if (p->per_chirp || p->sample_recs_ready) return TDC_OK;
+    const int C = p->C, S = p->S;
+    std::vector<ChirpRec> recs((size_t)C * S);
+    parallel_chirps(C, S, [&](int, int cb, int ce) {
+        for (int c = cb; c < ce; ++c)
+            for (int s = 0; s < S; ++s)
+                recs[(size_t)c * S + s] = make_record(p, c, s, p->opts.centroid != 0, p->opts.center);
+    });
+    TDC_CK(p->chirps.ensure(recs.size() * sizeof(ChirpRec)), "alloc per-sample records");
+    TDC_CK(cudaMemcpyAsync(p->chirps.p, recs.data(), recs.size() * sizeof(ChirpRec), cudaMemcpyHostToDevice,
+                           p->stream),
+           "copy per-sample records");
+    TDC_CK(cudaStreamSynchronize(p->stream), "per-sample records sync");
+    p->stats.h2d_bytes += (int64_t)(recs.size() * sizeof(ChirpRec));
+    p->sample_recs_ready = true;
+    return TDC_OK;
+}
+
 int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 {
     if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
@@ -660,6 +677,8 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     const int path = choose_path(p);
     const long long P = p->P;
     const int C = p->C;
+    if (path == TDC_PATH_GENERAL_FP64)
+        if (int rc = sample_records(p)) return rc;
 
     int cb = 1;
     const int variant = path == TDC_PATH_GENERAL ? general_variant(p) : 0;

@@ -152,6 +152,7 @@ struct tdc_processor {
     tdc::impl::StartOpts opts;
     bool per_chirp = true;
     bool traj_varies = false;   // positions differ within a chirp (FP32 per-sample positions)
+    bool sample_recs_ready = false;  // chirps holds the per-(chirp, sample) records
     bool win_varies = false;    // the Doppler window can differ within a chirp (finite band, per-sample motion)
     double delta_max = 0.0;     // max |P[c,s] - P[c,0]| [m]
     double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
