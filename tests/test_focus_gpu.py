@@ -411,3 +411,17 @@ def test_per_sample_motion_without_window_effect_takes_bulk_path(cuda_device):
     assert stats["path_name"] == "fp32_bulk"
     ref = _oracle(api, sc.grid, args).reshape(img.shape)
     _check(img, ref)
+
+
+@pytest.mark.parametrize("n_samples,nx,ny", [(1, 7, 5), (17, 1, 1), (33, 23, 29), (1500, 9, 4)])
+def test_fp32_general_kernel_odd_sizes(cuda_device, n_samples, nx, ny):
+    """General kernel on ragged shapes: one sample, one pixel, partial tiles, long chirps
+    (positions and windows per sample, jittered sample times)."""
+    sc = scenes.small_scene(seed=51 + n_samples, n_pri=140, n_samples=n_samples, nx=nx, ny=ny, device="cuda")
+    api = _general_api(sc, traj=True, win=True, nonunif=n_samples > 1)
+    args = (0.0, 30.0, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    # one sample per chirp cannot vary within the chirp: the bulk kernel takes it
+    assert stats["path_name"] == ("general" if n_samples > 1 else "fp32_bulk")
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref, l2=2e-4, phase=None)
