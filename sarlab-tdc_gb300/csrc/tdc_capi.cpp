@@ -284,10 +284,11 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
     const int s_pad = (int)round_up((size_t)S, kSampleAlign);
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
-    std::vector<float> gres(s_pad, 0.f);
+    std::vector<float> gres(2 * (size_t)s_pad, 0.f);  // residuals, then 2 f_s / c0
     for (int s = 0; s < S; ++s) {
         const double gsv = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
         gres[s] = (float)(gsv - (g0 + g1 * s));
+        gres[(size_t)s_pad + s] = (float)gsv;
     }
     std::vector<float4> traj, wins;
     p->traj_varies = pos_differ;
@@ -311,8 +312,8 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                     const float *ps = p->pos + 3 * ti(c, s);
                     const double dx = (double)ps[0] - p0[0], dy = (double)ps[1] - p0[1], dz = (double)ps[2] - p0[2];
                     m = std::max(m, dx * dx + dy * dy + dz * dz);
-                    const double gsv = g0 + g1 * s + (double)gres[s];
-                    traj[(size_t)c * s_pad + s] = make_float4((float)dx, (float)dy, (float)dz, (float)gsv);
+                    traj[(size_t)c * s_pad + s] =
+                        make_float4((float)dx, (float)dy, (float)dz, (float)(dx * dx + dy * dy + dz * dz));
                 }
             }
             d2[t] = m;
@@ -400,9 +401,9 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     TDC_CK(cudaMemcpyAsync(p->gs.p, gs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "copy freq table");
     TDC_CK(cudaMemcpyAsync(p->pos_base.p, base.data(), (size_t)C * 24, cudaMemcpyHostToDevice, st),
            "copy base positions");
-    TDC_CK(p->gres.ensure((size_t)s_pad * 4), "alloc residual frequency table");
-    TDC_CK(cudaMemcpyAsync(p->gres.p, gres.data(), (size_t)s_pad * 4, cudaMemcpyHostToDevice, st),
-           "copy residual frequency table");
+    TDC_CK(p->gres.ensure(gres.size() * 4), "alloc per-sample frequency tables");
+    TDC_CK(cudaMemcpyAsync(p->gres.p, gres.data(), gres.size() * 4, cudaMemcpyHostToDevice, st),
+           "copy per-sample frequency tables");
     if (!traj.empty()) {
         TDC_CK(p->traj.ensure(traj.size() * sizeof(float4)), "alloc per-sample offsets");
         TDC_CK(cudaMemcpyAsync(p->traj.p, traj.data(), traj.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
@@ -413,7 +414,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         TDC_CK(cudaMemcpyAsync(p->wins.p, wins.data(), wins.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
                "copy per-sample windows");
     }
-    p->stats.h2d_bytes += (int64_t)s_pad * 4 + (int64_t)((traj.size() + wins.size()) * sizeof(float4));
+    p->stats.h2d_bytes += (int64_t)gres.size() * 4 + (int64_t)((traj.size() + wins.size()) * sizeof(float4));
     p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)C * sizeof(ChirpRec) +
                           (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
@@ -622,6 +623,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     job.traj = p->traj_varies ? p->traj.as<const float4>() : nullptr;
     job.wins = p->win_varies ? p->wins.as<const float4>() : nullptr;
     job.gres = p->gres.as<const float>();
+    job.gsam = p->gres.as<const float>() + p->s_pad;
     job.grid_hi = p->grid_hi.as<const float4>();
     job.grid_lo = p->grid_lo_valid ? p->grid_lo.as<const float4>() : nullptr;
     job.skip = p->skip.as<const SkipPoint>();

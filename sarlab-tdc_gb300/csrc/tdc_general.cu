@@ -15,8 +15,9 @@
 // The first term is the bulk kernel's alpha + beta s, evaluated with the same
 // blocked Horner recurrence (H <- H QL + sum_k x'_k p_k). The rest, psi_s, is a
 // per-(pixel, sample) correction folded into the sample: x'_s = x_s w_s e^{j 2 pi psi_s}.
-// d_s comes without cancellation from the per-sample offset D_s = P[c,s] - P[c,0]:
-//   N = D.(2 (P0 - T) + D) = R_s^2 - R0^2,   d_s = N / (R0 + R_s) = (N / 2R0) f(N / R0^2),
+// d_s comes without cancellation from the per-sample offset D_s = P[c,s] - P[c,0]
+// (host table: D_s and |D_s|^2 per (chirp, sample)):
+//   N = 2 (P0 - T).D + |D|^2 = R_s^2 - R0^2,   d_s = N / (R0 + R_s) = (N / 2R0) f(N / R0^2),
 //   f(e) = 2 / (1 + sqrt(1 + e)) = 1 - e/4 + e^2/8 - 5e^3/64 + 7e^4/128 - ...,
 // the series taken to e^2 when the host bounds |e| <= 0.02 and |psi| <= 4 cycles (then
 // the sincos takes psi unreduced: its argument scaling adds < 2e-6 rad), else to e^4 with
@@ -76,7 +77,9 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
     __shared__ FocusJob sJ;
 
     GenShared &sp = *reinterpret_cast<GenShared *>(smem + kStages * stage_bytes);
-    float *sres = reinterpret_cast<float *>(smem + kStages * stage_bytes + sizeof(GenShared));
+    // per-sample tables of the unit: residual r_s [cycles/m] and g_s (2 pi g_s in the narrow
+    // variants, whose phase correction goes to the sincos in radians)
+    float *const sres = reinterpret_cast<float *>(smem + kStages * stage_bytes + sizeof(GenShared));
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -104,6 +107,7 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
         const int CB = sJ.stage_chirps;
         const int nblk = (c1 - c0 + CB - 1) / CB;
         const int s_pad = sJ.s_pad;
+        float *const sgs = sres + s_pad;
         const uint32_t xrow = static_cast<uint32_t>(s_pad) * 8u;
         const uint32_t arow = static_cast<uint32_t>(s_pad) * 16u;
         // stage layout: [CB x rows][CB trajectory rows][CB window rows][CB records]
@@ -152,8 +156,11 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
             sp.t[i * 6 + 4][tid] = lo.y;
             sp.t[i * 6 + 5][tid] = lo.z;
         }
-        if (WIDE) {
-            for (int s = tid; s < s_pad; s += kT) sres[s] = sJ.gres[s];
+        if (WIDE || TRAJ) {
+            for (int s = tid; s < s_pad; s += kT) {
+                if (WIDE) sres[s] = sJ.gres[s];
+                if (TRAJ) sgs[s] = WIDE ? sJ.gsam[s] : kTwoPiF * sJ.gsam[s];
+            }
             __syncthreads();
         }
 
@@ -270,14 +277,15 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
                         if (TRAJ) av = as[s];
                         if (WIN) bv = bs[s];
                         const float res = WIDE ? sres[s] : 0.0f;
+                        const float gsv = TRAJ ? sgs[s] : 0.0f;
 #pragma unroll
                         for (int i = 0; i < kPT; ++i) {
                             float yr = xr, yi = xi;
                             if (TRAJ || WIDE) {
                                 float psi = 0.0f;
                                 if (TRAJ) {
-                                    const float nx = av.x + t2x[i], ny = av.y + t2y[i], nz = av.z + t2z[i];
-                                    const float n = fmaf(av.x, nx, fmaf(av.y, ny, av.z * nz));
+                                    // N = 2 (P0 - T).D + |D|^2 (|D|^2 from the table)
+                                    const float n = fmaf(t2x[i], av.x, fmaf(t2y[i], av.y, fmaf(t2z[i], av.z, av.w)));
                                     const float e = n * b2[i];
                                     float f;
                                     if (WIDE) {
@@ -288,14 +296,15 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
                                         f = fmaf(e, 0.125f, -0.25f);
                                     }
                                     f = fmaf(f, e, 1.0f);
-                                    psi = av.w * ((n * a2[i]) * f);  // g_s d_s
+                                    psi = (gsv * a2[i]) * (n * f);  // g_s d_s (radians when narrow)
                                 }
                                 if (WIDE) {
                                     psi = fmaf(res, r0[i], psi);
                                     psi -= round_small(psi);
+                                    psi *= kTwoPiF;
                                 }
                                 float sn, cs;
-                                __sincosf(kTwoPiF * psi, &sn, &cs);
+                                __sincosf(psi, &sn, &cs);
                                 yr = fmaf(xr, cs, -xi * sn);
                                 yi = fmaf(xr, sn, xi * cs);
                             }
@@ -390,7 +399,7 @@ KernelFn select_kernel(int variant)
 
 int focus_general_smem_bytes(int stage_bytes, int s_pad)
 {
-    return kStages * stage_bytes + (int)sizeof(GenShared) + s_pad * (int)sizeof(float);
+    return kStages * stage_bytes + (int)sizeof(GenShared) + 2 * s_pad * (int)sizeof(float);
 }
 
 int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad)
