@@ -321,12 +321,16 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         p->delta_max = std::sqrt(*std::max_element(d2.begin(), d2.begin() + nt));
     }
     if (p->win_varies) {
+        // In band units: velocity x (-2 / lambda) / B and window centre / B, so the kernel forms
+        // (fDop - centre) / B with one dot product and one fused multiply-add.
         wins.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+        const double vs = -2.0 / (double)p->lambda / (double)o.bw, cs = 1.0 / (double)o.bw;
         parallel_chirps(C, S, [&](int, int cb, int ce) {
             for (int c = cb; c < ce; ++c)
                 for (int s = 0; s < S; ++s) {
                     const ChirpRec r = make_record(p, c, s, o.centroid != 0, o.center);
-                    wins[(size_t)c * s_pad + s] = make_float4(r.vel.x, r.vel.y, r.vel.z, r.p_hi.w);
+                    wins[(size_t)c * s_pad + s] = make_float4((float)(r.vel.x * vs), (float)(r.vel.y * vs),
+                                                              (float)(r.vel.z * vs), (float)(r.p_hi.w * cs));
                 }
         });
     }

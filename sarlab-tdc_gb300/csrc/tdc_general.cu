@@ -66,8 +66,10 @@ __device__ __forceinline__ float round_small(float v)
     return (v + kMagic) - kMagic;
 }
 
+// The window-and-residual variant without per-sample positions keeps more samples in
+// flight than 128 registers hold: it runs one CTA per SM instead of spilling.
 template <bool TRAJ, bool WIN, bool WIDE>
-__global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
+__global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_MINB)
     focus_general_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                          int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
 {
@@ -217,8 +219,8 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
 
                 float2 p[kPT][kL - 1];
                 float2 ql[kPT], q0[kPT], h[kPT];
-                float t2x[kPT], t2y[kPT], t2z[kPT];  // 2 (P0 - T) (TRAJ); P0 - T (WIN)
-                float r0[kPT], a2[kPT], b2[kPT], ir[kPT];  // R0, 1/2R0, 1/R0^2, 1/R0
+                float t2x[kPT], t2y[kPT], t2z[kPT];
+                float r0[kPT], a2[kPT], b2[kPT];  // R0, 1/2R0, 1/R0^2
 #pragma unroll
                 for (int i = 0; i < kPT; ++i) {
                     float dxh, dxl, dyh, dyl, dzh, dzl;
@@ -252,14 +254,15 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
                     __sincosf(kTwoPiF * alpha, &sa, &ca);
                     q0[i] = make_float2(w * ca, w * sa);
                     h[i] = make_float2(0.f, 0.f);
-                    const float sc = TRAJ ? 2.0f : 1.0f;
+                    // TRAJ: 2 (P0 - T) for the range change; else the unit vector (P0 - T) / R0
+                    // of the per-sample window
+                    const float sc = TRAJ ? 2.0f : rs;
                     t2x[i] = sc * dxh;
                     t2y[i] = sc * dyh;
                     t2z[i] = sc * dzh;
                     r0[i] = rh;
                     a2[i] = 0.5f * rs;  // 1 / 2R0
                     b2[i] = rs * rs;    // 1 / R0^2
-                    ir[i] = rs;         // 1 / R0
                 }
 
                 // Horner over blocks, last block first; each sample corrected per pixel.
@@ -309,13 +312,22 @@ __global__ void __launch_bounds__(kT, TDC_GENERAL_MINB)
                                 yi = fmaf(xr, sn, xi * cs);
                             }
                             if (WIN) {
-                                // per-sample window at P[c,s]: d = P0 - T + D_s
-                                const float dx = TRAJ ? fmaf(0.5f, t2x[i], av.x) : t2x[i];
-                                const float dy = TRAJ ? fmaf(0.5f, t2y[i], av.y) : t2y[i];
-                                const float dz = TRAJ ? fmaf(0.5f, t2z[i], av.z) : t2z[i];
-                                const float rsi = TRAJ ? rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) : ir[i];
-                                const float fd = doppler_freq(tol, bv.x, bv.y, bv.z, dx, dy, dz, rsi);
-                                const float w = doppler_window(fd, bv.w, half_bw, inv_bw, taper, az_a);
+                                // per-sample window at P[c,s] (d = P0 - T + D_s) in band units:
+                                // q = (fDop - centre) / B from the table's velocity scaled by
+                                // -2/(lambda B) and centre / B; in band for |q| <= 1/2, taper
+                                // a - (1-a) cos(2 pi q - pi) = a + (1-a) cos(2 pi q)
+                                float q;
+                                if (TRAJ) {
+                                    const float dx = fmaf(0.5f, t2x[i], av.x);
+                                    const float dy = fmaf(0.5f, t2y[i], av.y);
+                                    const float dz = fmaf(0.5f, t2z[i], av.z);
+                                    const float rsi = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                                    q = fmaf(fmaf(bv.x, dx, fmaf(bv.y, dy, bv.z * dz)), rsi, -bv.w);
+                                } else {
+                                    q = fmaf(bv.x, t2x[i], fmaf(bv.y, t2y[i], fmaf(bv.z, t2z[i], -bv.w)));
+                                }
+                                float w = taper ? fmaf(1.0f - az_a, __cosf(kTwoPiF * q), az_a) : 1.0f;
+                                w = fabsf(q) <= 0.5f ? w : 0.0f;
                                 yr *= w;
                                 yi *= w;
                             }

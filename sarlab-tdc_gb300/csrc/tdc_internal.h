@@ -66,7 +66,8 @@ struct FocusJob {
     const SkipPoint *skip;   // [n_chunks][9]
     const double *gs;        // [S] 2 f_s / c0 (FP64 kernels only)
     const float4 *traj;      // [C][s_pad] (P[c,s] - P[c,0], |P[c,s] - P[c,0]|^2) (FP32 general kernel, per-sample positions)
-    const float4 *wins;      // [C][s_pad] (velocity, window centre) per sample (FP32 general kernel, per-sample windows)
+    const float4 *wins;      // [C][s_pad] (velocity x -2/(lambda B), window centre / B) per sample (FP32 general
+                             // kernel, per-sample windows)
     const float *gres;       // [s_pad] 2 f_s / c0 - (g0 + g1 s) (FP32 general kernel, non-uniform sampling)
     const float *gsam;       // [s_pad] 2 f_s / c0 [cycles / m] (FP32 general kernel, per-sample positions)
     float4 *partial;         // [n_groups][P]: (sum.re, sum.im, comp.re, comp.im)
