@@ -25,6 +25,35 @@ def _arr(x, dtype):
     return np.ascontiguousarray(np.asarray(x).astype(dtype, copy=False))
 
 
+_TYPESTR = {"complex64": ("<c8", 8), "float64": ("<f8", 8)}
+
+
+def _device_buffer(obj, dtype: str, n_elems: int, what: str) -> int:
+    """Device address of a CUDA buffer holding at least n_elems contiguous elements of dtype:
+    a torch tensor, any object with __cuda_array_interface__ (CuPy, Numba, ...), or a raw
+    address (int, taken as is). Undersized, strided or mistyped buffers are refused, since
+    the kernels write n_elems elements."""
+    if isinstance(obj, int):
+        return obj
+    typestr, size = _TYPESTR[dtype]
+    if hasattr(obj, "data_ptr") and hasattr(obj, "is_cuda"):  # torch
+        import torch
+
+        want = {"complex64": torch.complex64, "float64": torch.float64}[dtype]
+        if not obj.is_cuda or obj.dtype != want or not obj.is_contiguous() or obj.numel() < n_elems:
+            raise ValueError(f"{what} must be a contiguous CUDA {dtype} tensor of at least {n_elems} elements")
+        return obj.data_ptr()
+    cai = getattr(obj, "__cuda_array_interface__", None)
+    if cai is None:
+        raise ValueError(f"{what} must be a CUDA array (torch tensor or __cuda_array_interface__) or an address")
+    count = int(np.prod(cai["shape"])) if cai["shape"] else 1
+    contiguous = cai.get("strides") is None or cai["strides"] == tuple(
+        int(np.prod(cai["shape"][i + 1:])) * size for i in range(len(cai["shape"])))
+    if cai["typestr"] != typestr or not contiguous or count < n_elems:
+        raise ValueError(f"{what} must be a contiguous {dtype} CUDA array of at least {n_elems} elements")
+    return int(cai["data"][0])
+
+
 def _check_image_array(out, rows, cols):
     if not isinstance(out, np.ndarray) or out.dtype != np.complex64 or out.shape != (rows, cols) \
             or not out.flags.c_contiguous or not out.flags.writeable:
@@ -235,21 +264,21 @@ class TdcProcessor:
 
     def focusDevice(self, image, stream=None):
         """Focus the resident acquisition onto the resident grid into ``image``
-        (a complex64 CUDA tensor of numPixels() elements, or a device address),
-        asynchronously on ``stream`` (default: torch's current stream)."""
-        addr = image if isinstance(image, int) else image.data_ptr()
+        (complex64, numPixels() elements: a CUDA tensor, any __cuda_array_interface__ array,
+        or a device address), asynchronously on ``stream`` (default: torch's current stream)."""
+        addr = _device_buffer(image, "complex64", self.numPixels(), "image")
         _lib.check(_lib.lib().tdc_processor_focus_device(self._h, addr, self._stream(stream)))
 
     def setChirpOffsetsDevice(self, offsets, stream=None):
         """Antenna positions := base + offsets (a CUDA float64 tensor [nPri, 3] or None)."""
-        addr = None if offsets is None else (offsets if isinstance(offsets, int) else offsets.data_ptr())
+        addr = None if offsets is None else _device_buffer(offsets, "float64", 3 * self.numChirps(), "offsets")
         _lib.check(_lib.lib().tdc_processor_set_chirp_offsets_device(self._h, addr, self._stream(stream)))
 
     def adjointDevice(self, grad_image, grad_offsets, stream=None):
         """grad_offsets [nPri, 3] float64 (CUDA) <- adjoint of focusDevice applied to grad_image
         (complex64 CUDA, dL/dRe I + j dL/dIm I). Blocking."""
-        gi = grad_image if isinstance(grad_image, int) else grad_image.data_ptr()
-        go = grad_offsets if isinstance(grad_offsets, int) else grad_offsets.data_ptr()
+        gi = _device_buffer(grad_image, "complex64", self.numPixels(), "grad_image")
+        go = _device_buffer(grad_offsets, "float64", 3 * self.numChirps(), "grad_offsets")
         _lib.check(_lib.lib().tdc_processor_adjoint_device(self._h, gi, go, self._stream(stream)))
 
     def check(self, stream=None):

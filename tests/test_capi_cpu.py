@@ -171,3 +171,28 @@ def test_wait_timeout_selftest_rejects_bad_limits_before_any_cuda_call(engine_li
         assert engine_lib.tdc_selftest_wait_timeout(0, limit, C.byref(flag), None) == _tdc_capi.TDC_ERR_INVALID_ARGUMENT
     assert engine_lib.tdc_selftest_wait_timeout(0, 1000, None, None) == _tdc_capi.TDC_ERR_INVALID_ARGUMENT
     assert flag.value == 7
+
+
+def test_device_buffers_are_checked_before_any_kernel_writes_them():
+    """focusDevice / adjointDevice / setChirpOffsetsDevice validate a CUDA array's dtype,
+    contiguity and size (the kernels write every element) -- checked here with fake
+    __cuda_array_interface__ objects, no GPU needed."""
+    import _sarlabtdc as S
+
+    class Fake:
+        def __init__(self, shape, typestr, strides=None, ptr=0x1000):
+            self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "strides": strides,
+                                             "data": (ptr, False), "version": 3}
+
+    assert S._device_buffer(Fake((100,), "<c8"), "complex64", 100, "image") == 0x1000
+    assert S._device_buffer(Fake((10, 10), "<c8", strides=(80, 8)), "complex64", 100, "image") == 0x1000
+    assert S._device_buffer(0x2000, "complex64", 100, "image") == 0x2000
+    with pytest.raises(ValueError):
+        S._device_buffer(Fake((99,), "<c8"), "complex64", 100, "image")          # too small
+    with pytest.raises(ValueError):
+        S._device_buffer(Fake((100,), "<c16"), "complex64", 100, "image")        # wrong dtype
+    with pytest.raises(ValueError):
+        S._device_buffer(Fake((100,), "<c8", strides=(16,)), "complex64", 100, "image")  # strided
+    with pytest.raises(ValueError):
+        S._device_buffer(np.zeros(100, np.complex64), "complex64", 100, "image")  # host array
+    assert S._device_buffer(Fake((7, 3), "<f8"), "float64", 21, "offsets") == 0x1000
