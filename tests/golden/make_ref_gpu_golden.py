@@ -114,7 +114,11 @@ def per_sample(a, n_pri, n_samples):
     return np.ascontiguousarray(a)
 
 
-def reference_focus(drv, case):
+def reference_focus(drv, case, host_skip=True, device_sum=False):
+    """The reference's per-(chunk, pixel) launch sequence. host_skip=False leaves out the
+    host skip test (it passes every chunk under an infinite band); device_sum=True keeps
+    the chunk sums and the image on the device (FP64 sum rounded to complex float, then
+    added, as nppsSum_32fc + addToImage do) instead of adding them on the host."""
     import torch
 
     import oracle
@@ -144,6 +148,7 @@ def reference_focus(drv, case):
     vel_st = np.zeros((CHUNK, S, 3), np.float32)
     att_st = np.zeros((CHUNK, S, 4), np.float32)
     image = np.zeros(grid.shape[0], np.complex64)
+    image_d = torch.zeros(grid.shape[0], dtype=torch.complex64, device=dev) if device_sum else None
     grid_blk = ((S + 15) // 16, CHUNK // 16)
     for k in range((C_ + CHUNK - 1) // CHUNK):
         valid = min(CHUNK, C_ - k * CHUNK)
@@ -155,7 +160,8 @@ def reference_focus(drv, case):
         att_d.copy_(torch.from_numpy(att_st.ravel()))
         for pix in range(grid.shape[0]):
             tgt = grid[pix]
-            if not skip_nonzero(pos_st, vel_st, att_st, S, tgt.astype(np.float64), bore, lam, center, bw, centroid):
+            if host_skip and not skip_nonzero(pos_st, vel_st, att_st, S, tgt.astype(np.float64), bore, lam, center,
+                                              bw, centroid):
                 continue
             T = F3(*[float(x) for x in tgt])
             B = F3(*bore)
@@ -167,10 +173,14 @@ def reference_focus(drv, case):
                        [ptr(ref_d), ptr(win_d), ptr(pos_d), ptr(st_d), T, C.c_float(f0), C.c_float(K), C.c_int(k),
                         C.c_int(C_), C.c_int(S)])
             drv.launch(K_CORR, grid_blk, (16, 16), [ptr(raw_d), ptr(ref_d), C.c_int(k), C.c_int(C_), C.c_int(S)])
+            if device_sum:
+                v = ref_d[: 2 * valid * S].view(-1, 2).double().sum(0).float()
+                image_d[pix] += torch.complex(v[0], v[1])
+                continue
             v = ref_d[: 2 * valid * S].view(-1, 2).double().sum(0).cpu().numpy()
             image[pix] = np.complex64(image[pix] + np.complex64(complex(v[0], v[1])))
     torch.cuda.synchronize()
-    return image
+    return image_d.cpu().numpy() if device_sum else image
 
 
 def make_cases():

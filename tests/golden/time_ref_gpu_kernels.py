@@ -1,0 +1,83 @@
+"""Time the reference's own GPU kernels on a pixel sample of the small stripmap workload
+and compare the engine's image with theirs.
+
+Like make_ref_gpu_golden.py (whose loader and launch sequence it reuses), this runs on a
+machine with a GPU and oracle/_ref/tdckernels.ptx (built by oracle/build.py from the
+reference's tdc-lib/src/tdckernels.cu). The reference's host loop
+(tdc-lib/src/tdcprocessor.cpp:59-167) needs spdlog and NPP, so it is emulated from Python
+in the same order -- per chunk of 128 PRIs and per pixel: window, reference response and
+correlation kernels, then a device sum added to the pixel on the device -- which is, if
+anything, lighter than the reference's per-call NPP context set-up. The pixel sample's
+time gives the reference path's per-pixel cost; Gcorr/s = chirps x samples / that cost.
+
+    python tests/golden/time_ref_gpu_kernels.py [n_pixels]
+
+Prints one JSON line.
+"""
+from __future__ import annotations
+
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+import make_ref_gpu_golden as ref  # noqa: E402
+
+
+def main() -> int:
+    import torch
+
+    from oracle import build as ob
+    from sarlabtdc import scenes
+
+    n_pix = int(sys.argv[1]) if len(sys.argv) > 1 else 256
+    ptx = ob.build_ref_ptx()
+    if ptx is None or not Path(ptx).exists():
+        print(json.dumps({"error": "oracle/_ref/tdckernels.ptx is missing"}))
+        return 1
+    drv = ref.Driver(Path(ptx).read_bytes())
+    sc = scenes.config1(device="cuda")
+    C_, S = sc.n_pri, sc.n_samples
+    rng = np.random.default_rng(7)
+    flat = sc.grid.reshape(-1, 3)
+    pix = np.sort(rng.choice(flat.shape[0], n_pix, replace=False))
+    case = dict(raw=sc.raw, sample_times=sc.radar.sample_times(), pos=sc.positions.astype(np.float32),
+                vel=np.zeros((C_, 3), np.float32), att=np.tile([1, 0, 0, 0], (C_, 1)).astype(np.float32),
+                grid=flat[pix].astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
+                start_freq=np.float32(sc.radar.f0), center=0.0, bw=float("inf"), centroid=0, apply_range_win=0,
+                taper=1, bore=np.array([0, 1, 0], np.float32))
+    # infinite band: the host skip test passes every chunk; sums stay on the device
+    ref.reference_focus(drv, dict(case, grid=case["grid"][:4]), host_skip=False, device_sum=True)  # warm-up
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    img_ref = ref.reference_focus(drv, case, host_skip=False, device_sum=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    per_px = dt / n_pix
+
+    import _sarlabtdc
+
+    p = _sarlabtdc.TdcProcessor(0)
+    api = sc.api_arrays()
+    p.setRawData(*api.values())
+    p.setFocusGrid(np.ascontiguousarray(case["grid"].reshape(1, -1, 3)))
+    p.start(0.0, float("inf"), False, False, True)
+    img = p.getFocusedImage().ravel()
+    err = float(np.linalg.norm(img - img_ref) / np.linalg.norm(img_ref))
+    out = {"workload": f"256x256 px stripmap, {C_} chirps x {S} samples (pixel sample)", "pixels": n_pix,
+           "reference_kernels_ms_per_pixel": round(per_px * 1e3, 4),
+           "reference_kernels_gcorr_s": round(C_ * S / per_px / 1e9, 4),
+           "reference_kernels_full_image_s": round(per_px * flat.shape[0], 2),
+           "engine_vs_reference_rel_l2": err,
+           "launches_per_pixel": 3 * ((C_ + ref.CHUNK - 1) // ref.CHUNK)}
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
