@@ -425,3 +425,33 @@ def test_fp32_general_kernel_odd_sizes(cuda_device, n_samples, nx, ny):
     assert stats["path_name"] == ("general" if n_samples > 1 else "fp32_bulk")
     ref = _oracle(api, sc.grid, args).reshape(img.shape)
     _check(img, ref, l2=2e-4, phase=None)
+
+
+def test_processors_on_concurrent_threads_match_sequential_runs(cuda_device):
+    """Processors with different sample counts (different kernel launch shapes and shared-
+    memory sizes) focusing at the same time from several host threads give the images they
+    give one at a time."""
+    import threading
+
+    scs = [scenes.small_scene(seed=61 + k, n_pri=300 + 37 * k, n_samples=S, nx=30, ny=20, device="cuda")
+           for k, S in enumerate((64, 200, 513, 1024))]
+    args = (0.0, INF, False, True, True)
+    alone = [run_engine(sc.api_arrays(), sc.grid, args)[0] for sc in scs]
+    out = [None] * len(scs)
+    errors = []
+
+    def work(k):
+        try:
+            for _ in range(3):
+                out[k] = run_engine(scs[k].api_arrays(), scs[k].grid, args)[0]
+        except Exception as e:  # noqa: BLE001
+            errors.append(e)
+
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(len(scs))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    assert not errors, errors
+    for a, b in zip(alone, out):
+        np.testing.assert_array_equal(a, b)
