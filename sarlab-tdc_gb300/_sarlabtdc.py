@@ -233,18 +233,22 @@ class TdcProcessor:
 
     def setImageOutput(self, image):
         """Caller-owned image output: later start() calls write the image straight into
-        ``image`` (C-contiguous complex64 [rows, cols] for the grid set at start), in place
-        from the GPU where it reads and writes host memory coherently, else by one copy.
-        ``None`` returns to the processor's own buffer. The array is kept alive here."""
+        ``image`` (a C-contiguous complex64 host array -- numpy, a CPU torch tensor, or any
+        __array_interface__ object -- of at least rows x cols elements for the grid set at
+        start), in place from the GPU where it reads and writes host memory coherently, else
+        by one copy. ``None`` returns to the processor's own buffer. The array is kept alive
+        here."""
         if image is None:
             _lib.check(_lib.lib().tdc_processor_set_image_output(self._h, None, 0))
             self._image_out = None
             return
-        if not isinstance(image, np.ndarray) or image.dtype != np.complex64 or not image.flags.c_contiguous \
-                or not image.flags.writeable:
-            raise ValueError("image output must be a writeable C-contiguous complex64 numpy array")
-        _lib.check(_lib.lib().tdc_processor_set_image_output(self._h, image.ctypes.data, int(image.size) * 2))
-        self._image_out = image
+        # numpy arrays, CPU torch tensors (pinned or not) and other __array_interface__ objects
+        # are taken as views of their own memory
+        arr = image if isinstance(image, np.ndarray) else np.asarray(image)
+        if arr.dtype != np.complex64 or not arr.flags.c_contiguous or not arr.flags.writeable:
+            raise ValueError("image output must be a writeable C-contiguous complex64 host array")
+        _lib.check(_lib.lib().tdc_processor_set_image_output(self._h, arr.ctypes.data, int(arr.size) * 2))
+        self._image_out = (image, arr)
 
     def readsHostMemory(self) -> bool:
         """True when the kernels read the input arrays in place over a coherent host link."""

@@ -338,6 +338,13 @@ def test_image_output_into_caller_buffer(cuda_device, monkeypatch, host_reads):
     np.testing.assert_array_equal(p.getFocusedImage(), ref)
     with pytest.raises(ValueError):
         p.setImageOutput(np.zeros((4, 4), np.complex128))
+    # a pinned CPU torch tensor as the output (a view of its memory, no copy through numpy)
+    import torch
+
+    t = torch.zeros(ref.shape, dtype=torch.complex64).pin_memory()
+    p.setImageOutput(t)
+    p.start(*args)
+    np.testing.assert_array_equal(t.numpy(), ref)
 
 
 def _general_api(sc, traj=False, win=False, nonunif=False, drift=0.3e-3, seed=5):
