@@ -1,5 +1,5 @@
-"""Time the reference's own GPU kernels on a pixel sample of the small stripmap workload
-and compare the engine's image with theirs.
+"""Time the reference's own GPU kernels on a pixel sample of a focus workload and compare
+the engine's image with theirs.
 
 Like make_ref_gpu_golden.py (whose loader and launch sequence it reuses), this runs on a
 machine with a GPU and oracle/_ref/tdckernels.ptx (built by oracle/build.py from the
@@ -10,9 +10,11 @@ correlation kernels, then a device sum added to the pixel on the device -- which
 anything, lighter than the reference's per-call NPP context set-up. The pixel sample's
 time gives the reference path's per-pixel cost; Gcorr/s = chirps x samples / that cost.
 
-    python tests/golden/time_ref_gpu_kernels.py [n_pixels]
+    python tests/golden/time_ref_gpu_kernels.py [workload] [n_pixels]
 
-Prints one JSON line.
+workload 1: the 256^2 stripmap (1024 chirps x 512 samples); 2: the precision study
+(1024^2, 4096 x 1024; its FP64 positions and grid given to both as FP32, the reference's
+input type); 3: the 3-D volume (16384 x 256). Prints one JSON line.
 """
 from __future__ import annotations
 
@@ -35,13 +37,14 @@ def main() -> int:
     from oracle import build as ob
     from sarlabtdc import scenes
 
-    n_pix = int(sys.argv[1]) if len(sys.argv) > 1 else 256
+    workload = sys.argv[1] if len(sys.argv) > 1 else "1"
+    n_pix = int(sys.argv[2]) if len(sys.argv) > 2 else 256
     ptx = ob.build_ref_ptx()
     if ptx is None or not Path(ptx).exists():
         print(json.dumps({"error": "oracle/_ref/tdckernels.ptx is missing"}))
         return 1
     drv = ref.Driver(Path(ptx).read_bytes())
-    sc = scenes.config1(device="cuda")
+    sc = {"1": scenes.config1, "2": scenes.config2, "3": scenes.config3}[workload](device="cuda")
     C_, S = sc.n_pri, sc.n_samples
     rng = np.random.default_rng(7)
     flat = sc.grid.reshape(-1, 3)
@@ -69,7 +72,8 @@ def main() -> int:
     p.start(0.0, float("inf"), False, False, True)
     img = p.getFocusedImage().ravel()
     err = float(np.linalg.norm(img - img_ref) / np.linalg.norm(img_ref))
-    out = {"workload": f"256x256 px stripmap, {C_} chirps x {S} samples (pixel sample)", "pixels": n_pix,
+    out = {"workload": f"workload {workload}: {flat.shape[0]} px, {C_} chirps x {S} samples (pixel sample)",
+           "pixels": n_pix,
            "reference_kernels_ms_per_pixel": round(per_px * 1e3, 4),
            "reference_kernels_gcorr_s": round(C_ * S / per_px / 1e9, 4),
            "reference_kernels_full_image_s": round(per_px * flat.shape[0], 2),
