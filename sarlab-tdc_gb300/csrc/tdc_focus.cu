@@ -267,22 +267,34 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 const ChirpRec r = recs[cc];
                 const float4 *xs = xs_stage + (size_t)cc * (s_pad / 2);
 
-                float2 p[kFocusPT][kL - 1];
-                float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
+                // Range and window first: a chirp whose window (Doppler band, skip test) is
+                // zero for every pixel of the warp contributes nothing and is skipped.
+                float rh[kFocusPT], rl[kFocusPT], w[kFocusPT];
+                bool live = false;
 #pragma unroll
                 for (int i = 0; i < kFocusPT; ++i) {
                     float dxh, dxl, dyh, dyl, dzh, dzl;
                     dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
                     dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
                     dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
-                    float rh, rl, rs, dh;
-                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
-                    const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
+                    float rs, dh;
+                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh[i], rl[i], rs, dh);
+                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                    w[i] = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                    live |= w[i] != 0.0f;
+                }
+                if (!__any_sync(0xffffffffu, live)) continue;
+
+                float2 p[kFocusPT][kL - 1];
+                float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
+#pragma unroll
+                for (int i = 0; i < kFocusPT; ++i) {
+                    const float alpha = dd_frac_mul(g0h, g0l, rh[i], rl[i]);
                     // beta = (g1 + g1l) * (rh + rl) cycles per sample, reduced modulo 1.
-                    float bh = g1 * rh;
-                    float bl = fmaf(g1, rh, -bh);
-                    bl = fmaf(g1, rl, bl);
-                    bl = fmaf(g1l, rh, bl);
+                    float bh = g1 * rh[i];
+                    float bl = fmaf(g1, rh[i], -bh);
+                    bl = fmaf(g1, rl[i], bl);
+                    bl = fmaf(g1l, rh[i], bl);
                     bh -= rintf(bh);
                     float s1, c1s;
                     __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
@@ -294,11 +306,9 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     float sl, cl;
                     sincospif(2.0f * lfr, &sl, &cl);
                     ql[i] = make_float2(cl, sl);
-                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
-                    const float w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
                     float sa, ca;
                     __sincosf(kTwoPiF * alpha, &sa, &ca);
-                    q0[i] = make_float2(w * ca, w * sa);
+                    q0[i] = make_float2(w[i] * ca, w[i] * sa);
                     h[i] = make_float2(0.f, 0.f);
                 }
 

@@ -93,7 +93,11 @@ __global__ void __launch_bounds__(kThreads) focus_fp64_kernel(const FocusJob *__
 #pragma unroll
         for (int i = 0; i < kPT; ++i) acc[i] = make_float2(0.f, 0.f);
 
-        if (!PER_SAMPLE) {
+        bool live = false;
+        if (PER_SAMPLE) {
+#pragma unroll
+            for (int i = 0; i < kPT; ++i) live |= wskip[i] != 0.0f;
+        } else {
             const ChirpRec rec = J.chirps[c];
             const double px = to_d(rec.p_hi.x, rec.p_lo.x), py = to_d(rec.p_hi.y, rec.p_lo.y),
                          pz = to_d(rec.p_hi.z, rec.p_lo.z);
@@ -105,8 +109,11 @@ __global__ void __launch_bounds__(kThreads) focus_fp64_kernel(const FocusJob *__
                 const float rs = rsqrtf(fdx * fdx + fdy * fdy + fdz * fdz);
                 const float fd = doppler_freq(tol, rec.vel.x, rec.vel.y, rec.vel.z, fdx, fdy, fdz, rs);
                 w[i] = wskip[i] * doppler_window(fd, rec.p_hi.w, half_bw, inv_bw, taper, az_a);
+                live |= w[i] != 0.0f;
             }
         }
+        // a chirp whose weight is zero for every pixel of the warp contributes nothing
+        if (!__any_sync(0xffffffffu, live)) continue;
 
         const float4 *__restrict__ row = xw + (size_t)c * (s_pad / 2);
         for (int s2 = 0; s2 < (S + 1) / 2; ++s2) {

@@ -221,6 +221,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                 float2 ql[kPT], q0[kPT], h[kPT];
                 float t2x[kPT], t2y[kPT], t2z[kPT];
                 float r0[kPT], a2[kPT], b2[kPT];  // R0, 1/2R0, 1/R0^2
+                bool live = false;
 #pragma unroll
                 for (int i = 0; i < kPT; ++i) {
                     float dxh, dxl, dyh, dyl, dzh, dzl;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                         const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
                         w *= doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
                     }
+                    live |= w != 0.0f;
                     float sa, ca;
                     __sincosf(kTwoPiF * alpha, &sa, &ca);
                     q0[i] = make_float2(w * ca, w * sa);
@@ -264,6 +266,9 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                     a2[i] = 0.5f * rs;  // 1 / 2R0
                     b2[i] = rs * rs;    // 1 / R0^2
                 }
+                // a chirp whose chirp-level weight (skip test, and the window unless it is
+                // per sample) is zero for every pixel of the warp contributes nothing
+                if (!__any_sync(0xffffffffu, live)) continue;
 
                 // Horner over blocks, last block first; each sample corrected per pixel.
                 for (int b = nb - 1; b >= 0; --b) {
