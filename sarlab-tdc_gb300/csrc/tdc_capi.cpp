@@ -803,7 +803,8 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     int *status = counter + 1;
     if (path == TDC_PATH_FP32_BULK) {
         const int grid = std::min(n_units, slots);
-        TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, st),
+        TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
+                                 std::isfinite(job.half_bw), st),
                "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);

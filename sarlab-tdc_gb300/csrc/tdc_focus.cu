@@ -90,6 +90,10 @@ __device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2
     return make_float2(tr, ti);
 }
 
+// SKIP_ZERO: chirps whose window is zero for a whole warp skip the Horner loop (launched
+// when a job's Doppler band is finite; with an unbounded band no window is zero, and the
+// plain instance keeps the hot loop's schedule).
+template <bool SKIP_ZERO>
 __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                       int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
@@ -267,9 +271,8 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 const ChirpRec r = recs[cc];
                 const float4 *xs = xs_stage + (size_t)cc * (s_pad / 2);
 
-                // Range and window first: a chirp whose window (Doppler band, skip test) is
-                // zero for every pixel of the warp contributes nothing and is skipped.
-                float rh[kFocusPT], rl[kFocusPT], w[kFocusPT];
+                float2 p[kFocusPT][kL - 1];
+                float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
                 bool live = false;
 #pragma unroll
                 for (int i = 0; i < kFocusPT; ++i) {
@@ -277,24 +280,14 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
                     dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
                     dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
-                    float rs, dh;
-                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh[i], rl[i], rs, dh);
-                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
-                    w[i] = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
-                    live |= w[i] != 0.0f;
-                }
-                if (!__any_sync(0xffffffffu, live)) continue;
-
-                float2 p[kFocusPT][kL - 1];
-                float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
-#pragma unroll
-                for (int i = 0; i < kFocusPT; ++i) {
-                    const float alpha = dd_frac_mul(g0h, g0l, rh[i], rl[i]);
+                    float rh, rl, rs, dh;
+                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
+                    const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
                     // beta = (g1 + g1l) * (rh + rl) cycles per sample, reduced modulo 1.
-                    float bh = g1 * rh[i];
-                    float bl = fmaf(g1, rh[i], -bh);
-                    bl = fmaf(g1, rl[i], bl);
-                    bl = fmaf(g1l, rh[i], bl);
+                    float bh = g1 * rh;
+                    float bl = fmaf(g1, rh, -bh);
+                    bl = fmaf(g1, rl, bl);
+                    bl = fmaf(g1l, rh, bl);
                     bh -= rintf(bh);
                     float s1, c1s;
                     __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
@@ -306,11 +299,17 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     float sl, cl;
                     sincospif(2.0f * lfr, &sl, &cl);
                     ql[i] = make_float2(cl, sl);
+                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                    const float w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                    if (SKIP_ZERO) live |= w != 0.0f;
                     float sa, ca;
                     __sincosf(kTwoPiF * alpha, &sa, &ca);
-                    q0[i] = make_float2(w[i] * ca, w[i] * sa);
+                    q0[i] = make_float2(w * ca, w * sa);
                     h[i] = make_float2(0.f, 0.f);
                 }
+                // A chirp whose window (Doppler band, skip test) is zero for every pixel of the
+                // warp contributes nothing: the Horner loop is skipped.
+                if (SKIP_ZERO && !__any_sync(0xffffffffu, live)) continue;
 
                 // Horner over blocks, last block first.
 #pragma unroll kUnrollBlocks
@@ -408,23 +407,33 @@ int focus_fp32_smem_bytes(int stage_bytes)
 int focus_fp32_blocks_per_sm(int stage_bytes)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    if (allow_max_dynamic_smem(focus_fp32_kernel) != cudaSuccess) return 0;
-    int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel, kFocusThreads, smem) !=
-        cudaSuccess) {
+    int blocks = 0, blocks_skip = 0;
+    if (allow_max_dynamic_smem(focus_fp32_kernel<false>) != cudaSuccess ||
+        allow_max_dynamic_smem(focus_fp32_kernel<true>) != cudaSuccess)
         return 0;
-    }
-    return blocks;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel<false>, kFocusThreads, smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_skip, focus_fp32_kernel<true>, kFocusThreads, smem) !=
+            cudaSuccess)
+        return 0;
+    return blocks < blocks_skip ? blocks : blocks_skip;
 }
 
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
-                              int *status_dev, int stage_bytes, int grid_ctas, cudaStream_t st)
+                              int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero, cudaStream_t st)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel);
-    if (e != cudaSuccess) return e;
-    focus_fp32_kernel<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
-                                                               status_dev, stage_bytes);
+    if (skip_zero) {
+        cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel<true>);
+        if (e != cudaSuccess) return e;
+        focus_fp32_kernel<true><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
+                                                                         status_dev, stage_bytes);
+    } else {
+        cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel<false>);
+        if (e != cudaSuccess) return e;
+        focus_fp32_kernel<false><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
+                                                                          status_dev, stage_bytes);
+    }
     return cudaGetLastError();
 }
 

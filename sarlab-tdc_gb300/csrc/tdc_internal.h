@@ -120,9 +120,10 @@ cudaError_t launch_grid_from_f32(const float *grid, long long P, float4 *hi, cud
 cudaError_t launch_grid_from_f64(const double *grid, long long P, float4 *hi, float4 *lo, cudaStream_t st);
 
 // FP32-bulk focus over a unit list. `jobs` and `units` are device arrays.
+// skip_zero: skip chirps whose window is zero for a whole warp (any job with a finite band).
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,
-                              cudaStream_t st);
+                              bool skip_zero, cudaStream_t st);
 // Plain FP64-phase focus (comparator and general fallback), one CTA per unit.
 cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *status_dev, int per_sample, cudaStream_t st);

@@ -340,6 +340,7 @@ void tdc_server::launch_batch()
     FocusJob *hj = reinterpret_cast<FocusJob *>(h + kBatchOffJobs);
     FocusUnit *hu = reinterpret_cast<FocusUnit *>(h + off_units);
     int stage_bytes = 0;
+    bool skip_zero = false;  // any job with a finite Doppler band
     b.finishing.clear();
     b.members = members;
     const double t = now_ms() - t0;
@@ -362,6 +363,7 @@ void tdc_server::launch_batch()
         Job *j = members[i];
         hj[i] = j->plan.job;
         stage_bytes = std::max(stage_bytes, j->plan.stage_bytes);
+        skip_zero = skip_zero || std::isfinite(j->plan.job.half_bw);
         j->next_unit += take[i];
         if (j->t_first < 0) j->t_first = t;
         if (j->next_unit == j->n_units) b.finishing.push_back(j);
@@ -373,7 +375,7 @@ void tdc_server::launch_batch()
     unsigned char *d = static_cast<unsigned char *>(b.dev.p);
     err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
                              reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
-                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, st) != cudaSuccess;
+                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, st) != cudaSuccess;
     err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess;
     stats.launches++;
     if (!b.finishing.empty() && batches[bi ^ 1].in_flight) {
