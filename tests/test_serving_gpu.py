@@ -136,3 +136,32 @@ def test_unbatched_general_path_job_in_a_mix(cuda_device):
     p.start(*START)
     assert p.lastStats()["path_name"] == "general"
     np.testing.assert_array_equal(p.getFocusedImage().ravel(), img)
+
+
+def test_finite_band_job_in_a_mix_keeps_every_image(cuda_device):
+    """A job with a finite Doppler band makes its launches use the zero-window-skipping kernel
+    instance; every job of the mix still gets its alone image bit for bit."""
+    from sarlabtdc.serving import FocusServer
+
+    jobs = _jobs()[:4]
+    band = scenes.small_scene(seed=14, n_pri=400, n_samples=64, nx=48, ny=24, rail_len=0.4, device="cuda")
+    vel = np.zeros((band.n_pri, 3), np.float32)
+    vel[:, 0] = 0.05
+    band_start = (0.0, 12.0, False, False, True)
+
+    def submit_band(srv):
+        return srv.submit(band.raw, band.radar.sample_times(), band.positions, band.grid,
+                          np.float32(band.radar.mod_rate), np.float32(band.radar.f0), velocity=vel,
+                          start=band_start)
+
+    with FocusServer(max_jobs=6) as srv:
+        alone = [srv.wait(_submit(srv, sc))[0] for sc in jobs]
+        band_alone = srv.wait(submit_band(srv))[0]
+        ids = [_submit(srv, sc) for sc in jobs]
+        bid = submit_band(srv)
+        mixed = [srv.wait(i)[0] for i in ids]
+        band_mixed = srv.wait(bid)[0]
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(a, m)
+    np.testing.assert_array_equal(band_alone, band_mixed)
+    assert np.abs(band_alone).max() > 0
