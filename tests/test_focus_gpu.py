@@ -462,3 +462,12 @@ def test_processors_on_concurrent_threads_match_sequential_runs(cuda_device):
     assert not errors, errors
     for a, b in zip(alone, out):
         np.testing.assert_array_equal(a, b)
+
+
+def test_empty_grid_gives_an_empty_image(cuda_device):
+    """A focus grid with no pixels: start() succeeds and the image is empty (the reference
+    loops over zero pixels)."""
+    sc = scenes.small_scene(seed=71, n_pri=64, n_samples=32, nx=4, ny=4, device="cuda")
+    img, stats, _ = run_engine(sc.api_arrays(), np.zeros((0, 5, 3), np.float32), (0.0, INF, False, True, True))
+    assert img.shape == (0, 5)
+    assert stats["correlations"] == 0
