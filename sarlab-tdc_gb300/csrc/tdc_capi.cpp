@@ -398,16 +398,30 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                                  cudaMemcpyHostToDevice, st),
                "copy raw data");
     }
-    TDC_CK(cudaMemcpyAsync(rec_buf.p, recs.data(), (size_t)C * sizeof(ChirpRec), cudaMemcpyHostToDevice, st),
-           "copy chirp records");
-    TDC_CK(cudaMemcpyAsync(p->skip.p, skip.data(), skip.size() * sizeof(SkipPoint), cudaMemcpyHostToDevice, st),
-           "copy skip table");
-    TDC_CK(cudaMemcpyAsync(p->gs.p, gs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "copy freq table");
-    TDC_CK(cudaMemcpyAsync(p->pos_base.p, base.data(), (size_t)C * 24, cudaMemcpyHostToDevice, st),
-           "copy base positions");
     TDC_CK(p->gres.ensure(gres.size() * 4), "alloc per-sample frequency tables");
-    TDC_CK(cudaMemcpyAsync(p->gres.p, gres.data(), gres.size() * 4, cudaMemcpyHostToDevice, st),
-           "copy per-sample frequency tables");
+    {
+        // The small per-acquisition tables go through one pinned staging buffer, so their
+        // copies are asynchronous DMA instead of staged pageable copies.
+        struct Piece {
+            void *dst;
+            const void *src;
+            size_t bytes;
+        };
+        const Piece pieces[] = {{rec_buf.p, recs.data(), (size_t)C * sizeof(ChirpRec)},
+                                {p->skip.p, skip.data(), skip.size() * sizeof(SkipPoint)},
+                                {p->gs.p, gs.data(), (size_t)S * 8},
+                                {p->pos_base.p, base.data(), (size_t)C * 24},
+                                {p->gres.p, gres.data(), gres.size() * 4}};
+        size_t total = 0;
+        for (const Piece &pc : pieces) total += round_up(pc.bytes, 256);
+        TDC_CK(p->table_host.ensure(total), "alloc pinned table staging");
+        unsigned char *h = static_cast<unsigned char *>(p->table_host.p);
+        for (const Piece &pc : pieces) {
+            std::memcpy(h, pc.src, pc.bytes);
+            TDC_CK(cudaMemcpyAsync(pc.dst, h, pc.bytes, cudaMemcpyHostToDevice, st), "copy acquisition tables");
+            h += round_up(pc.bytes, 256);
+        }
+    }
     if (!traj.empty()) {
         TDC_CK(p->traj.ensure(traj.size() * sizeof(float4)), "alloc per-sample offsets");
         TDC_CK(cudaMemcpyAsync(p->traj.p, traj.data(), traj.size() * sizeof(float4), cudaMemcpyHostToDevice, st),

@@ -182,6 +182,7 @@ struct tdc_processor {
 
     tdc::impl::DevBuf image_dev;
     tdc::impl::PinnedBuf image_host;
+    tdc::impl::PinnedBuf table_host;  // staging of the per-acquisition tables (prepare)
     float *image_out = nullptr;  // caller-owned image output (borrowed), or null
     int64_t image_out_floats = 0;
     bool image_valid = false;
