@@ -73,6 +73,33 @@ __global__ void rows_differ_kernel(const unsigned int *__restrict__ a, int C, in
     if (__syncthreads_or(differ) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
+// The same test reading 16 bytes per load (a 16-byte aligned, C x S x k < 2^31 elements):
+// the arrays usually sit in the caller's host memory, where wide loads move them faster.
+__global__ void rows_differ_vec_kernel(const uint4 *__restrict__ a4, unsigned int total, unsigned int per,
+                                       unsigned int k, int *__restrict__ flag)
+{
+    const unsigned int *a = reinterpret_cast<const unsigned int *>(a4);
+    const unsigned int n4 = total / 4;
+    bool differ = false;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const uint4 v = a4[i];
+        const unsigned int w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const unsigned int e = 4 * i + q;
+            const unsigned int c = e / per;
+            const unsigned int r = e - c * per;
+            differ |= w[q] != a[c * per + r % k];
+        }
+    }
+    for (unsigned int e = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const unsigned int c = e / per;
+        const unsigned int r = e - c * per;
+        differ |= a[e] != a[c * per + r % k];
+    }
+    if (__syncthreads_or(differ) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 // Bounding box of the grid's high floats: out = (min x, min y, min z, max x, max y, max z),
 // each as an order-preserving int (see float_key); out must start at (INT_MAX x3, INT_MIN x3).
 __device__ __forceinline__ int float_key(float f)
@@ -179,6 +206,15 @@ cudaError_t launch_rows_differ(const float *a, int C, int S, int k, int *flag, c
 {
     const long long total = (long long)C * S * k;
     if (total <= 0) return cudaSuccess;
+    if ((reinterpret_cast<uintptr_t>(a) & 15u) == 0 && total < (1LL << 31)) {
+        long long blocks = (total / 4 + 255) / 256;
+        if (blocks > 152 * 16) blocks = 152 * 16;
+        if (blocks < 1) blocks = 1;
+        rows_differ_vec_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const uint4 *>(a),
+                                                                (unsigned)total, (unsigned)((long long)S * k),
+                                                                (unsigned)k, flag);
+        return cudaGetLastError();
+    }
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     rows_differ_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const unsigned int *>(a), C, S, k, flag);
