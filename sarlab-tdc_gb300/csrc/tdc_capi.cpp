@@ -208,12 +208,29 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     if (!p->has_raw) return fail(TDC_ERR_STATE, "setRawData must be called before start()");
     const int C = p->C, S = p->S;
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
+    const int s_pad = (int)round_up((size_t)S, kSampleAlign);
+    cudaStream_t st = p->stream;
+
+    // Where the device reads the caller's buffers in place, the raw rows are windowed
+    // and padded on the GPU while the host analyses the trajectory (launched right
+    // after the trajectory scan, which the host waits for through an event).
+    auto window_raw_in_place = [&]() -> int {
+        TDC_CK(p->xw.ensure((size_t)C * s_pad * 8), "alloc samples");
+        TDC_CK(p->wr.ensure((size_t)S * 4), "alloc range window");
+        TDC_CK(launch_range_window(p->wr.as<float>(), S, o.range_win, st), "range window kernel");
+        TDC_CK(launch_prewindow_from(reinterpret_cast<const float2 *>(p->raw), p->wr.as<float>(), C, S, s_pad,
+                                     p->xw.as<float2>(), st),
+               "prewindow kernel");
+        launches += 2;
+        return TDC_OK;
+    };
 
     // ---- host analysis ----
     // Trajectory element of (chirp c, sample s): per-sample arrays, or one row per chirp.
     const bool tpc = p->traj_per_chirp;
     auto ti = [tpc, S](long c, long s) -> size_t { return tpc ? (size_t)c : (size_t)c * S + s; };
     bool pos_differ = false, motion_differ = false;
+    bool raw_windowed = false;
     if (tpc) {
         p->per_chirp = true;
     } else if (p->host_reads) {
@@ -228,7 +245,10 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         if (p->att) TDC_CK(launch_rows_differ(p->att, C, S, 4, flag + 1, p->stream), "scan kernel");
         int differ[2] = {0, 0};
         TDC_CK(cudaMemcpyAsync(differ, flag, 8, cudaMemcpyDeviceToHost, p->stream), "read flag");
-        TDC_CK(cudaStreamSynchronize(p->stream), "scan sync");
+        TDC_CK(cudaEventRecord(p->ev[5], p->stream), "event");
+        if (int rc = window_raw_in_place()) return rc;
+        raw_windowed = true;
+        TDC_CK(cudaEventSynchronize(p->ev[5]), "scan sync");
         pos_differ = differ[0] != 0;
         motion_differ = differ[1] != 0;
         launches += (!p->pos64) + (p->vel != nullptr) + (p->att != nullptr);
@@ -237,6 +257,8 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         motion_differ = !rows_constant(p->vel, C, S, 3) || !rows_constant(p->att, C, S, 4);
     }
     if (!tpc) p->per_chirp = !pos_differ && !motion_differ;
+    if (p->host_reads && !raw_windowed)
+        if (int rc = window_raw_in_place()) return rc;
     fit_frequencies(p->sample_times, S, p->start_freq, p->mod_rate, p->F0, p->F1, p->resid_hz);
     for (int k = 0; k < 3; ++k) {
         p->ant_min[k] = std::numeric_limits<double>::infinity();
@@ -282,7 +304,6 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     p->sample_recs_ready = false;
 
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
-    const int s_pad = (int)round_up((size_t)S, kSampleAlign);
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
     std::vector<float> gres(2 * (size_t)s_pad, 0.f);  // residuals, then 2 f_s / c0
     for (int s = 0; s < S; ++s) {
@@ -382,7 +403,6 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     // ---- device buffers ----
     p->s_pad = s_pad;
     p->n_chunks = n_chunks;
-    cudaStream_t st = p->stream;
     TDC_CK(p->xw.ensure((size_t)C * s_pad * 8), "alloc samples");
     TDC_CK(p->wr.ensure((size_t)S * 4), "alloc range window");
     // sample-0 records go to gen_rec when the trajectory varies within chirps (chirps then
@@ -437,16 +457,11 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                           (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
 
-    TDC_CK(launch_range_window(p->wr.as<float>(), S, o.range_win, st), "range window kernel");
-    if (p->host_reads) {
-        // Window and pad straight from the caller's buffer (read over the coherent host link).
-        TDC_CK(launch_prewindow_from(reinterpret_cast<const float2 *>(p->raw), p->wr.as<float>(), C, S, s_pad,
-                                     p->xw.as<float2>(), st),
-               "prewindow kernel");
-    } else {
+    if (!p->host_reads) {
+        TDC_CK(launch_range_window(p->wr.as<float>(), S, o.range_win, st), "range window kernel");
         TDC_CK(launch_prewindow(p->xw.as<float2>(), p->wr.as<float>(), C, S, s_pad, st), "prewindow kernel");
+        launches += 2;
     }
-    launches += 2;
     // The host vectors above are read by the async copies: wait before they go out of scope.
     TDC_CK(cudaStreamSynchronize(st), "prepare sync");
 
