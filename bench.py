@@ -349,7 +349,7 @@ def run_ours(args):
     import oracle
 
     build_oracle()
-    pix = sample_pixels(sc, 192)
+    pix = sample_pixels(sc, 1024)
     t = time.time()
     ref = oracle.focus(oracle_problem(sc, api, f64), oracle_opts(), pixels=pix)
     got = image[pix]
