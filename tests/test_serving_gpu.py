@@ -165,3 +165,52 @@ def test_finite_band_job_in_a_mix_keeps_every_image(cuda_device):
         np.testing.assert_array_equal(a, m)
     np.testing.assert_array_equal(band_alone, band_mixed)
     assert np.abs(band_alone).max() > 0
+
+
+def test_many_small_jobs_from_several_client_threads(cuda_device):
+    """Four client threads submit and wait on 400 small jobs in an interleaved order; every
+    image equals the processor's image of the same job bit for bit."""
+    import threading
+
+    import _sarlabtdc
+    from sarlabtdc.serving import FocusServer
+
+    base = [scenes.small_scene(seed=200 + k, n_pri=64 + 16 * k, n_samples=32 + 8 * k, nx=16 + k, ny=12,
+                               device="cuda") for k in range(6)]
+    ref = []
+    for sc in base:
+        p = _sarlabtdc.TdcProcessor(0)
+        p.setRawData(*sc.api_arrays().values())
+        p.setChirpPositionsF64(sc.positions)
+        p.setFocusGridF64(sc.grid)
+        p.start(*START)
+        ref.append(p.getFocusedImage().ravel().copy())
+    bad, errors = [], []
+
+    def client(tid, srv):
+        try:
+            rng = np.random.default_rng(tid)
+            pending = []
+            for _ in range(100):
+                k = int(rng.integers(len(base)))
+                pending.append((_submit(srv, base[k]), k))
+                if rng.random() < 0.3:
+                    j, kk = pending.pop(0)
+                    if not np.array_equal(srv.wait(j)[0], ref[kk]):
+                        bad.append(j)
+            for j, kk in pending:
+                if not np.array_equal(srv.wait(j)[0], ref[kk]):
+                    bad.append(j)
+        except Exception as e:  # noqa: BLE001
+            errors.append(e)
+
+    with FocusServer(max_jobs=8) as srv:
+        ths = [threading.Thread(target=client, args=(t, srv)) for t in range(4)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        st = srv.stats()
+    assert not errors, errors
+    assert not bad
+    assert st["jobs_done"] == 400 and st["jobs_failed"] == 0
