@@ -242,6 +242,30 @@ def make_cases():
                                grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
                                start_freq=np.float32(sc.radar.f0), center=0.0, bw=float("inf"), centroid=0,
                                apply_range_win=1, taper=1, bore=np.array([0, 1, 0], np.float32))
+    # F: one sample per chirp, 130 PRIs (a last chunk of two rows, the rest stale), moving
+    # antenna, centroid window with taper
+    rng = np.random.default_rng(109)
+    sc = scenes.small_scene(seed=110, n_pri=130, n_samples=1, nx=9, ny=7, rail_len=0.2, device="cuda")
+    vel = np.zeros((130, 3), np.float32)
+    vel[:, 0] = 0.06
+    yaw = rng.normal(0, 0.03, 130)
+    att = np.stack([np.cos(yaw / 2), 0 * yaw, 0 * yaw, np.sin(yaw / 2)], 1).astype(np.float32)
+    # (a one-sample Hann window is zero: seeded complex Gaussian samples instead)
+    raw1 = (rng.normal(size=(130, 1)) + 1j * rng.normal(size=(130, 1))).astype(np.complex64)
+    cases["onesample"] = dict(raw=raw1, sample_times=sc.radar.sample_times(), pos=sc.positions.astype(np.float32),
+                              vel=vel, att=att, grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
+                              start_freq=np.float32(sc.radar.f0), center=1.0, bw=22.0, centroid=1,
+                              apply_range_win=1, taper=1, bore=np.array([0, 1, 0], np.float32))
+    # G: 17 samples per chirp (odd, not a multiple of the engine's 8-sample blocks), 75 PRIs
+    # (a single partial chunk), reference range window, rectangular window, fixed centre
+    sc = scenes.small_scene(seed=111, n_pri=75, n_samples=17, nx=11, ny=6, rail_len=0.15, device="cuda")
+    vel = np.zeros((75, 3), np.float32)
+    vel[:, 0] = 0.03
+    cases["odd"] = dict(raw=sc.raw, sample_times=sc.radar.sample_times(), pos=sc.positions.astype(np.float32),
+                        vel=vel, att=np.tile([1, 0, 0, 0], (75, 1)).astype(np.float32),
+                        grid=sc.grid.astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
+                        start_freq=np.float32(sc.radar.f0), center=-1.0, bw=16.0, centroid=0, apply_range_win=1,
+                        taper=0, bore=np.array([0, 1, 0], np.float32))
     return cases
 
 

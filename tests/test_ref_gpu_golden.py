@@ -1,6 +1,6 @@
 """Parity against the reference's own GPU output.
 
-tests/golden/ref_gpu_images.npz holds five small acquisitions and the images
+tests/golden/ref_gpu_images.npz holds seven small acquisitions and the images
 the reference's kernels (tdc-lib/src/tdckernels.cu, compiled from its source to
 PTX and launched in the order of tdcprocessor.cpp:59-167) produced for them on a
 GB300; tests/golden/make_ref_gpu_golden.py made it. The oracle (CPU) and the
