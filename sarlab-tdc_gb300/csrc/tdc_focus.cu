@@ -45,11 +45,6 @@ namespace {
 #ifndef TDC_FOCUS_SWAP
 #define TDC_FOCUS_SWAP 0
 #endif
-// 1: stages are released per warp on "empty" mbarriers instead of a CTA barrier per
-// stage (warps drift up to kFocusStages - 1 stages apart).
-#ifndef TDC_FOCUS_EMPTYBAR
-#define TDC_FOCUS_EMPTYBAR 0
-#endif
 
 constexpr int kL = TDC_FOCUS_L;  // in-block phasor table length
 constexpr int kUnrollBlocks = TDC_FOCUS_UNROLL;
@@ -100,9 +95,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar[kFocusStages];
-#if TDC_FOCUS_EMPTYBAR
-    __shared__ uint64_t empty_bar[kFocusStages];
-#endif
     __shared__ int s_unit;
     __shared__ FocusJob sJ;
 
@@ -111,12 +103,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     const int tid = threadIdx.x;
 
     if (tid == 0) {
-        for (int i = 0; i < kFocusStages; ++i) {
-            mbar_init(&full_bar[i], 1);
-#if TDC_FOCUS_EMPTYBAR
-            mbar_init(&empty_bar[i], kFocusThreads / 32);
-#endif
-        }
+        for (int i = 0; i < kFocusStages; ++i) mbar_init(&full_bar[i], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -203,49 +190,15 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
         }
         int cur_chunk = -1;
         bool timed_out = false;
-#if TDC_FOCUS_EMPTYBAR
-        int next_issue = nblk < kFocusStages ? nblk : kFocusStages;  // producer (thread 0) only
-#endif
 
         for (int j = 0; j < nblk; ++j) {
             const int st = n_consumed % kFocusStages;
             const uint32_t parity = (n_consumed / kFocusStages) & 1u;
-#if TDC_FOCUS_EMPTYBAR
-            if (tid == 0) {
-                // Refill buffers the warps have released: stage j must be issued before it is
-                // awaited; later ones go as soon as their buffer is free.
-                while (next_issue < nblk) {
-                    const int b = n_issued % kFocusStages;
-                    const uint32_t ep = ((n_issued - kFocusStages) / kFocusStages) & 1u;
-                    if (next_issue <= j) {
-                        if (!mbar_wait_bounded(&empty_bar[b], ep, kWaitLimitNs)) break;
-                    } else if (!mbar_try_wait(&empty_bar[b], ep)) {
-                        break;
-                    }
-                    const int cb0n = c0 + next_issue * CB;
-                    const int cntn = min(CB, c1 - cb0n);
-                    unsigned char *basen = smem + b * stage_bytes;
-                    const uint32_t bx = cntn * row_bytes, br = cntn * (uint32_t)sizeof(ChirpRec);
-                    fence_proxy_async_smem();
-                    mbar_arrive_expect_tx(&full_bar[b], bx + br);
-                    bulk_g2s(basen, xw + (size_t)cb0n * (s_pad / 2), bx, &full_bar[b]);
-                    bulk_g2s(basen + CB * row_bytes, chirps + cb0n, br, &full_bar[b]);
-                    ++n_issued;
-                    ++next_issue;
-                }
-            }
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full_bar[st], parity, kWaitLimitNs));
-            if (!ok) {
-                timed_out = true;
-                break;
-            }
-#else
             const bool ok = mbar_wait_bounded(&full_bar[st], parity, kWaitLimitNs);
             if (__syncthreads_or(!ok)) {
                 timed_out = true;
                 break;
             }
-#endif
             const unsigned char *base = smem + st * stage_bytes;
             const float4 *xs_stage = reinterpret_cast<const float4 *>(base);
             const ChirpRec *recs = reinterpret_cast<const ChirpRec *>(base + CB * row_bytes);
@@ -334,11 +287,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 }
             }
 
-#if TDC_FOCUS_EMPTYBAR
-            __syncwarp();
-            if ((tid & 31) == 0) mbar_arrive(&empty_bar[st]);  // this warp is done with the stage
-            ++n_consumed;
-#else
             __syncthreads();  // every thread is done with this stage
             ++n_consumed;
             if (tid == 0 && j + kFocusStages < nblk) {
@@ -354,11 +302,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 bulk_g2s(basen + CB * row_bytes, chirps + cb0n, br, &full_bar[stn]);
                 ++n_issued;
             }
-#endif
         }
-#if TDC_FOCUS_EMPTYBAR
-        timed_out = __syncthreads_or(timed_out);  // warps leave the stage loop independently
-#endif
 
         if (timed_out) {
             // Let the copies still in flight land before the CTA exits, then report.
