@@ -87,6 +87,8 @@ constexpr double kGeneralMaxEps = 0.1;
 constexpr double kGeneralNarrowEps = 0.02;
 constexpr double kGeneralNarrowCycles = 4.0;
 constexpr int kGeneralStageTarget = 32768;
+// Long chirps: samples per staged segment when a whole row does not fit the bulk kernel's stages.
+constexpr int kSegmentSamples = 2048;
 
 }  // namespace impl
 }  // namespace tdc
@@ -573,11 +575,9 @@ int choose_path(const tdc_processor *p)
     const bool fp64 = p->precision == TDC_PRECISION_FP64_PHASE;
     if (variant == 0) {
         // One record per chirp describes every sample (a per-sample trajectory whose
-        // variation cannot change the phase or the window is focused like a per-chirp one).
+        // variation cannot change the phase or the window is focused like a per-chirp one);
+        // rows too long for the stages are staged in segments.
         if (fp64) return p->per_chirp ? TDC_PATH_FP64_PHASE : TDC_PATH_GENERAL_FP64;
-        if (focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)p->s_pad * 8 + sizeof(ChirpRec), 128) >
-            227 * 1024)
-            return TDC_PATH_GENERAL_FP64;
         return TDC_PATH_FP32_BULK;
     }
     if (fp64) return TDC_PATH_GENERAL_FP64;
@@ -635,6 +635,12 @@ int stage_bytes_for(int s_pad, int &cb)
     const int row = s_pad * 8 + (int)sizeof(ChirpRec);
     cb = std::max(1, kFocusStageTarget / row);
     return (int)round_up((size_t)cb * row, 128);
+}
+
+bool needs_segments(int s_pad)
+{
+    return focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)s_pad * 8 + sizeof(ChirpRec), 128) >
+           226 * 1024;
 }
 
 int general_stage_bytes_for(int s_pad, int variant, int &cb)
@@ -717,11 +723,13 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 
     int cb = 1;
     const int variant = path == TDC_PATH_GENERAL ? general_variant(p) : 0;
-    const int stage_bytes =
-        path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, cb) : stage_bytes_for(p->s_pad, cb);
+    const bool seg = path == TDC_PATH_FP32_BULK && needs_segments(p->s_pad);
+    const int stage_bytes = path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, cb)
+                            : seg ? (int)round_up((size_t)kSegmentSamples * 8 + sizeof(ChirpRec), 128)
+                                  : stage_bytes_for(p->s_pad, cb);
     int slots;
     if (path == TDC_PATH_FP32_BULK) {
-        const int bps = focus_fp32_blocks_per_sm(stage_bytes);
+        const int bps = seg ? focus_fp32_seg_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
         slots = p->n_sm * bps;
     } else if (path == TDC_PATH_GENERAL) {
@@ -764,12 +772,14 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     unsigned char *scr = p->scratch.as<unsigned char>();
     plan.path = path;
     plan.variant = variant;
+    plan.seg = seg;
     plan.cb = cb;
     plan.stage_bytes = stage_bytes;
     plan.slots = slots;
     plan.off_job = L.off_job;
     plan.off_units = L.off_units;
     plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
+    plan.job.seg_len = seg ? kSegmentSamples : 0;
     return TDC_OK;
 }
 
@@ -832,9 +842,14 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     int *status = counter + 1;
     if (path == TDC_PATH_FP32_BULK) {
         const int grid = std::min(n_units, slots);
-        TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
-                                 std::isfinite(job.half_bw), st),
-               "focus kernel");
+        if (plan.seg)
+            TDC_CK(launch_focus_fp32_seg(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
+                                         std::isfinite(job.half_bw), st),
+                   "focus kernel (segmented rows)");
+        else
+            TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
+                                     std::isfinite(job.half_bw), st),
+                   "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);
         TDC_CK(launch_focus_general(plan.variant, jobs_dev, units_dev, n_units, counter, status, stage_bytes,
@@ -1210,6 +1225,8 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     if (!p->per_chirp || choose_path(p) != TDC_PATH_FP32_BULK)
         return fail(TDC_ERR_UNSUPPORTED, "the adjoint needs the FP32-bulk path (per-chirp trajectory, uniform "
                                          "sample spacing)");
+    if (needs_segments(p->s_pad))
+        return fail(TDC_ERR_UNSUPPORTED, "the adjoint stages whole chirps: these chirps are too long");
     TDC_CK(cudaSetDevice(p->device), "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long long P = p->P;

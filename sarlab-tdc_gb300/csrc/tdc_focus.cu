@@ -326,6 +326,228 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     }
 }
 
+// Long chirps: the same focus with a chirp's samples staged in segments of
+// job.seg_len samples (a row longer than the pipeline stages hold). Stages walk each
+// chirp's segments last first, so the Horner state of the chirp carries from one
+// segment to the next; the per-(pixel, chirp) set-up runs at the chirp's first staged
+// segment, the Kahan accumulation after its segment 0.
+template <bool SKIP_ZERO>
+__global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
+    focus_fp32_seg_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
+                          int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full_bar[kFocusStages];
+    __shared__ int s_unit;
+    __shared__ FocusJob sJ;
+
+    SharedPixel &sp = *reinterpret_cast<SharedPixel *>(smem + kFocusStages * stage_bytes);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int i = 0; i < kFocusStages; ++i) mbar_init(&full_bar[i], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    uint32_t n_issued = 0;
+    uint32_t n_consumed = 0;
+
+    for (;;) {
+        if (tid == 0) s_unit = atomicAdd(counter, 1);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= n_units) break;
+        const FocusUnit un = units[u];
+        if (tid < (int)(sizeof(FocusJob) / sizeof(int)))
+            reinterpret_cast<int *>(&sJ)[tid] = reinterpret_cast<const int *>(&jobs[un.job])[tid];
+        __syncthreads();
+
+        const int C = sJ.C;
+        const int c0 = un.group * sJ.chirps_per_group;
+        const int c1 = min(C, c0 + sJ.chirps_per_group);
+        const int s_pad = sJ.s_pad;
+        const int seg = sJ.seg_len;                 // samples per segment (multiple of 16)
+        const int nseg = (s_pad + seg - 1) / seg;
+        const int nstage = (c1 - c0) * nseg;
+        const uint32_t seg_bytes = static_cast<uint32_t>(seg) * 8u;
+        const float4 *__restrict__ xw = sJ.xw;
+        const ChirpRec *__restrict__ chirps = sJ.chirps;
+
+        // stage j: chirp c0 + j / nseg, segment nseg - 1 - j % nseg
+        auto issue = [&](int j) {
+            const int c = c0 + j / nseg;
+            const int sg = nseg - 1 - j % nseg;
+            const int off = sg * seg;
+            const int len = min(seg, s_pad - off);
+            const int st = n_issued % kFocusStages;
+            unsigned char *base = smem + st * stage_bytes;
+            const uint32_t bx = static_cast<uint32_t>(len) * 8u, br = (uint32_t)sizeof(ChirpRec);
+            mbar_arrive_expect_tx(&full_bar[st], bx + br);
+            bulk_g2s(base, xw + ((size_t)c * s_pad + off) / 2, bx, &full_bar[st]);
+            bulk_g2s(base + seg_bytes, chirps + c, br, &full_bar[st]);
+            ++n_issued;
+        };
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            const int npro = nstage < kFocusStages ? nstage : kFocusStages;
+            for (int j = 0; j < npro; ++j) issue(j);
+        }
+
+        const long long tile_base = (long long)un.tile * kFocusTile;
+        const long long P = sJ.P;
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            const long long p = tile_base + i * kFocusThreads + tid;
+            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+            if (p < P) {
+                hi = __ldg(&sJ.grid_hi[p]);
+                if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[p]);
+            }
+            sp.t[i * 6 + 0][tid] = hi.x;
+            sp.t[i * 6 + 1][tid] = hi.y;
+            sp.t[i * 6 + 2][tid] = hi.z;
+            sp.t[i * 6 + 3][tid] = lo.x;
+            sp.t[i * 6 + 4][tid] = lo.y;
+            sp.t[i * 6 + 5][tid] = lo.z;
+        }
+
+        const float g0h = sJ.g0_hi, g0l = sJ.g0_lo, g1 = sJ.g1, g1l = sJ.g1_lo;
+        const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
+        const bool taper = (sJ.flags & kFlagTaper) != 0;
+        const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
+        const int chunk = sJ.chunk;
+        const SkipPoint *__restrict__ skip = sJ.skip;
+
+        float2 sum[kFocusPT], comp[kFocusPT];
+        float wskip[kFocusPT];
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            sum[i] = make_float2(0.f, 0.f);
+            comp[i] = make_float2(0.f, 0.f);
+            wskip[i] = 1.0f;
+        }
+        float2 p[kFocusPT][kL - 1];
+        float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
+        bool live = true;
+        int cur_chunk = -1;
+        bool timed_out = false;
+
+        for (int j = 0; j < nstage; ++j) {
+            const int st = n_consumed % kFocusStages;
+            const uint32_t parity = (n_consumed / kFocusStages) & 1u;
+            const bool ok = mbar_wait_bounded(&full_bar[st], parity, kWaitLimitNs);
+            if (__syncthreads_or(!ok)) {
+                timed_out = true;
+                break;
+            }
+            const unsigned char *base = smem + st * stage_bytes;
+            const float4 *xs = reinterpret_cast<const float4 *>(base);
+            const int c = c0 + j / nseg;
+            const int sg = nseg - 1 - j % nseg;
+            const int len = min(seg, s_pad - sg * seg);
+
+            if (sg == nseg - 1) {
+                // first staged segment of the chirp: skip weight, range, phase set-up
+                if (skip_test) {
+                    const int k = c / chunk;
+                    if (k != cur_chunk) {
+                        cur_chunk = k;
+#pragma unroll
+                        for (int i = 0; i < kFocusPT; ++i)
+                            wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, sp.t[i * 6 + 0][tid],
+                                                        sp.t[i * 6 + 1][tid], sp.t[i * 6 + 2][tid], tol, half_bw)
+                                           ? 1.0f
+                                           : 0.0f;
+                    }
+                }
+                const ChirpRec r = *reinterpret_cast<const ChirpRec *>(base + seg_bytes);
+                bool any = false;
+#pragma unroll
+                for (int i = 0; i < kFocusPT; ++i) {
+                    float dxh, dxl, dyh, dyl, dzh, dzl;
+                    dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
+                    dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
+                    dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
+                    float rh, rl, rs, dh;
+                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
+                    const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
+                    float bh = g1 * rh;
+                    float bl = fmaf(g1, rh, -bh);
+                    bl = fmaf(g1, rl, bl);
+                    bl = fmaf(g1l, rh, bl);
+                    bh -= rintf(bh);
+                    float s1, c1s;
+                    __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
+                    p[i][0] = make_float2(c1s, s1);
+#pragma unroll
+                    for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
+                    const float lbh = (float)kL * bh;
+                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
+                    float sl, cl;
+                    sincospif(2.0f * lfr, &sl, &cl);
+                    ql[i] = make_float2(cl, sl);
+                    const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                    const float w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                    any |= w != 0.0f;
+                    float sa, ca;
+                    __sincosf(kTwoPiF * alpha, &sa, &ca);
+                    q0[i] = make_float2(w * ca, w * sa);
+                    h[i] = make_float2(0.f, 0.f);
+                }
+                live = !SKIP_ZERO || __any_sync(0xffffffffu, any);
+            }
+
+            if (live) {
+                // Horner over this segment's blocks, last block first
+                for (int b = len / kL - 1; b >= 0; --b) {
+                    float4 xv[kL / 2];
+#pragma unroll
+                    for (int m = 0; m < kL / 2; ++m) xv[m] = xs[b * (kL / 2) + m];
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) h[i] = horner_block(h[i], ql[i], p[i], xv);
+                }
+                if (sg == 0) {
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) {
+                        const float2 v = cmul(q0[i], h[i]);
+                        const float yr = v.x - comp[i].x, yi = v.y - comp[i].y;
+                        const float tr = sum[i].x + yr, ti = sum[i].y + yi;
+                        comp[i].x = (tr - sum[i].x) - yr;
+                        comp[i].y = (ti - sum[i].y) - yi;
+                        sum[i].x = tr;
+                        sum[i].y = ti;
+                    }
+                }
+            }
+
+            __syncthreads();  // every thread is done with this stage
+            ++n_consumed;
+            if (tid == 0 && j + kFocusStages < nstage) {
+                fence_proxy_async_smem();
+                issue(j + kFocusStages);
+            }
+        }
+
+        if (timed_out) {
+            if (tid == 0) {
+                for (uint32_t k = n_consumed; k < n_issued; ++k)
+                    mbar_wait_bounded(&full_bar[k % kFocusStages], (k / kFocusStages) & 1u, kWaitLimitNs);
+                atomicOr(status, kStatusTimeout);
+            }
+            __syncthreads();
+            return;
+        }
+
+        float4 *__restrict__ part = sJ.partial + (size_t)un.group * P;
+#pragma unroll
+        for (int i = 0; i < kFocusPT; ++i) {
+            const long long pidx = tile_base + i * kFocusThreads + tid;
+            if (pidx < P) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
+        }
+        __syncthreads();
+    }
+}
+
 // image[p] = sum over groups of (sum - comp), added in FP64 in group order.
 __global__ void focus_reduce_kernel(const float4 *__restrict__ partial, int n_groups, long long P,
                                     float2 *__restrict__ image)
@@ -378,6 +600,38 @@ cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_d
         focus_fp32_kernel<false><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
                                                                           status_dev, stage_bytes);
     }
+    return cudaGetLastError();
+}
+
+int focus_fp32_seg_blocks_per_sm(int stage_bytes)
+{
+    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    int blocks = 0, blocks_skip = 0;
+    if (allow_max_dynamic_smem(focus_fp32_seg_kernel<false>) != cudaSuccess ||
+        allow_max_dynamic_smem(focus_fp32_seg_kernel<true>) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_seg_kernel<false>, kFocusThreads, smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_skip, focus_fp32_seg_kernel<true>, kFocusThreads,
+                                                      smem) != cudaSuccess)
+        return 0;
+    return blocks < blocks_skip ? blocks : blocks_skip;
+}
+
+cudaError_t launch_focus_fp32_seg(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
+                                  int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero,
+                                  cudaStream_t st)
+{
+    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    cudaError_t e = skip_zero ? allow_max_dynamic_smem(focus_fp32_seg_kernel<true>)
+                              : allow_max_dynamic_smem(focus_fp32_seg_kernel<false>);
+    if (e != cudaSuccess) return e;
+    if (skip_zero)
+        focus_fp32_seg_kernel<true><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units,
+                                                                             counter_dev, status_dev, stage_bytes);
+    else
+        focus_fp32_seg_kernel<false><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units,
+                                                                              counter_dev, status_dev, stage_bytes);
     return cudaGetLastError();
 }
 

@@ -89,6 +89,8 @@ struct FocusJob {
     float inv_bw;            // 1 / dopplerBandwidth
     float az_a;              // azimuth window a
     float g1_lo;             // low part of g1 (double-float pair)
+    int seg_len;             // samples per pipeline stage of a chirp staged in segments (0: whole rows)
+    int pad_;
 };
 
 // Kernels copy a FocusJob into shared memory one int per thread (128 threads); the
@@ -120,6 +122,12 @@ cudaError_t launch_grid_from_f32(const float *grid, long long P, float4 *hi, cud
 cudaError_t launch_grid_from_f64(const double *grid, long long P, float4 *hi, float4 *lo, cudaStream_t st);
 
 // FP32-bulk focus over a unit list. `jobs` and `units` are device arrays.
+// Long chirps (rows longer than the stages hold): the same focus with rows staged in
+// segments of job.seg_len samples; stage_bytes >= seg_len x 8 + one record.
+cudaError_t launch_focus_fp32_seg(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
+                                  int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero,
+                                  cudaStream_t st);
+int focus_fp32_seg_blocks_per_sm(int stage_bytes);
 // skip_zero: skip chirps whose window is zero for a whole warp (any job with a finite band).
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,

@@ -205,6 +205,7 @@ namespace impl {
 struct FocusPlan {
     int path = 0;         // tdc_path
     int variant = 0;      // FP32 general kernel variant bits (TDC_PATH_GENERAL)
+    bool seg = false;     // FP32-bulk rows staged in segments (chirps longer than the stages hold)
     int cb = 1;           // chirps per pipeline stage
     int stage_bytes = 0;  // bytes per pipeline stage
     int slots = 0;        // resident CTAs of the kernel on the device
@@ -218,6 +219,8 @@ int upload_grid(tdc_processor *p, int &launches);
 int choose_path(const tdc_processor *p);
 void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg);
 int stage_bytes_for(int s_pad, int &cb);
+// True when a whole row of s_pad samples does not fit the FP32-bulk kernel's stages.
+bool needs_segments(int s_pad);
 // Stage bytes of the FP32 general kernel for a variant (bit 1 per-sample positions, 2 windows).
 int general_stage_bytes_for(int s_pad, int variant, int &cb);
 // Variant bits of the FP32 general kernel for the resident acquisition.

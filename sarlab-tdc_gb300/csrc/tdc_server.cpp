@@ -466,9 +466,11 @@ void tdc_server::admit_loop()
         const int rc = admit_one(j);
         int rc2 = TDC_OK;
         std::string err2;
-        if (!rc && j->plan.path != TDC_PATH_FP32_BULK) {
-            // FP64 / general path: not batched, focused on its own on the side stream (at the
-            // launch streams' priority, so it shares the SMs with the batches).
+        const bool batched = j->plan.path == TDC_PATH_FP32_BULK && !j->plan.seg;
+        if (!rc && !batched) {
+            // FP64 / general path or rows staged in segments: not batched, focused on its own
+            // on the side stream (at the launch streams' priority, so it shares the SMs with
+            // the batches).
             tdc_processor *p = j->slot;
             rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), side);
             if (rc2) {
@@ -488,7 +490,7 @@ void tdc_server::admit_loop()
             fail_job(j, rc, err);
         } else if (rc2) {
             fail_job(j, rc2, err2);
-        } else if (j->plan.path != TDC_PATH_FP32_BULK) {
+        } else if (!batched) {
             j->t_first = now_ms() - t0;
             j->state = kCompleting;
             completing.push_back(j);

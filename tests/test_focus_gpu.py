@@ -471,3 +471,17 @@ def test_empty_grid_gives_an_empty_image(cuda_device):
     img, stats, _ = run_engine(sc.api_arrays(), np.zeros((0, 5, 3), np.float32), (0.0, INF, False, True, True))
     assert img.shape == (0, 5)
     assert stats["correlations"] == 0
+
+
+@pytest.mark.parametrize("n_samples,band", [(9000, INF), (12000, 40.0), (20000, INF)])
+def test_long_chirps_are_staged_in_segments(cuda_device, n_samples, band):
+    """Rows longer than the bulk kernel's pipeline stages hold are staged in segments and
+    stay on the FP32-bulk path (parity with the oracle; a finite band takes the
+    zero-window-skipping instance)."""
+    sc = scenes.small_scene(seed=81, n_pri=40, n_samples=n_samples, nx=10, ny=8, rail_len=0.1, device="cuda")
+    api = _moving_api(sc, speed=0.05) if np.isfinite(band) else sc.api_arrays()
+    args = (0.0, band, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "fp32_bulk"
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    _check(img, ref, l2=2e-4 if np.isfinite(band) else L2_TOL, phase=None if np.isfinite(band) else PHASE_TOL)
