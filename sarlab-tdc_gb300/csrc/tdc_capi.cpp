@@ -723,10 +723,21 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 
     int cb = 1;
     const int variant = path == TDC_PATH_GENERAL ? general_variant(p) : 0;
-    const bool seg = path == TDC_PATH_FP32_BULK && needs_segments(p->s_pad);
+    // FP32-bulk rows are staged whole, or in segments when whole rows do not fit the stages
+    // or leave fewer CTAs per SM than segments do (long chirps).
+    const int seg_stage_bytes = (int)round_up((size_t)kSegmentSamples * 8 + sizeof(ChirpRec), 128);
+    bool seg = false;
+    if (path == TDC_PATH_FP32_BULK && p->s_pad > kSegmentSamples) {
+        seg = needs_segments(p->s_pad);
+        if (!seg) {
+            int cb_whole = 1;
+            seg = focus_fp32_blocks_per_sm(stage_bytes_for(p->s_pad, cb_whole)) <
+                  focus_fp32_seg_blocks_per_sm(seg_stage_bytes);
+        }
+    }
     const int stage_bytes = path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, cb)
-                            : seg ? (int)round_up((size_t)kSegmentSamples * 8 + sizeof(ChirpRec), 128)
-                                  : stage_bytes_for(p->s_pad, cb);
+                            : seg                     ? seg_stage_bytes
+                                                      : stage_bytes_for(p->s_pad, cb);
     int slots;
     if (path == TDC_PATH_FP32_BULK) {
         const int bps = seg ? focus_fp32_seg_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
