@@ -26,7 +26,10 @@
 // truncation is 4e-7 of d_s).
 //
 // Same unit decomposition, staging (cp.async.bulk + mbarrier pipeline), skip test,
-// Kahan accumulation and FP64 group reduction as the bulk kernel.
+// Kahan accumulation and FP64 group reduction as the bulk kernel; a chirp whose
+// chirp-level weight is zero for every pixel of a warp skips the Horner loop. The
+// per-sample window works in band units, q = (fDop - centre) / B, from a table of
+// velocities pre-scaled by -2 / (lambda B) and centres by 1 / B.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
