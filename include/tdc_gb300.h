@@ -133,6 +133,9 @@ typedef struct tdc_start_stats {
     int64_t correlations; /* pixels x chirps x samples */
     int path;             /* tdc_path used */
     int kernel_launches;  /* launches of this library's kernels inside start() */
+    int stage_samples;    /* samples of a chirp row per pipeline stage of the FP32 kernels
+                             (the whole row, or one segment of a long row; 0 on FP64 paths) */
+    int stage_chirps;     /* chirp rows per pipeline stage (1 when rows are staged in segments) */
 } tdc_start_stats;
 
 typedef enum tdc_path {

@@ -118,6 +118,8 @@ class StartStats(C.Structure):
         ("correlations", C.c_int64),
         ("path", C.c_int),
         ("kernel_launches", C.c_int),
+        ("stage_samples", C.c_int),
+        ("stage_chirps", C.c_int),
     ]
 
     def as_dict(self) -> dict:

@@ -307,11 +307,12 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
-    std::vector<float> gres(2 * (size_t)s_pad, 0.f);  // residuals, then 2 f_s / c0
+    std::vector<float> gres(3 * (size_t)s_pad, 0.f);  // residuals, 2 f_s / c0, 2 pi x 2 f_s / c0
     for (int s = 0; s < S; ++s) {
         const double gsv = 2.0 * ((double)p->start_freq + (double)p->mod_rate * (double)p->sample_times[s]) / kC0;
         gres[s] = (float)(gsv - (g0 + g1 * s));
         gres[(size_t)s_pad + s] = (float)gsv;
+        gres[2 * (size_t)s_pad + s] = (float)(2.0 * M_PI * gsv);
     }
     std::vector<float4> traj, wins;
     p->traj_varies = pos_differ;
@@ -584,10 +585,7 @@ int choose_path(const tdc_processor *p)
     // Per-sample range change d_s = N/(2 R0) f(N/R0^2): the series of f stays accurate for
     // |N/R0^2| <= 2 dmax/Rmin + (dmax/Rmin)^2 <= 0.1.
     if ((variant & 1) && !(range_change_bound(p) <= kGeneralMaxEps)) return TDC_PATH_GENERAL_FP64;
-    int cb = 1;
-    const int stage_bytes = general_stage_bytes_for(p->s_pad, variant, cb);
-    // 227 KiB of shared memory per CTA, less the kernel's static shared memory
-    if (focus_general_smem_bytes(stage_bytes, p->s_pad) > 226 * 1024) return TDC_PATH_GENERAL_FP64;
+    // rows of any length fit: those too long for whole-row stages are staged in segments
     return TDC_PATH_GENERAL;
 }
 
@@ -643,11 +641,51 @@ bool needs_segments(int s_pad)
            226 * 1024;
 }
 
-int general_stage_bytes_for(int s_pad, int variant, int &cb)
+namespace {
+
+// Bytes the FP32 general kernel stages per (chirp, sample): the raw sample, and the
+// trajectory and window table entries where the variant reads them.
+int general_row_bytes_per_sample(int variant)
 {
-    const int row = s_pad * (8 + ((variant & 1) ? 16 : 0) + ((variant & 2) ? 16 : 0)) + (int)sizeof(ChirpRec);
-    cb = std::max(1, kGeneralStageTarget / row);
-    return (int)round_up((size_t)cb * row, 128);
+    return 8 + ((variant & 1) ? 16 : 0) + ((variant & 2) ? 16 : 0);
+}
+
+// Bytes of the per-sample frequency tables staged with each row segment: the non-uniform
+// sampling residual (wide variants) and 2 f_s / c0 (per-sample positions).
+int general_table_bytes_per_sample(int variant)
+{
+    return ((variant & 4) ? 4 : 0) + ((variant & 1) ? 4 : 0);
+}
+
+}  // namespace
+
+int general_stage_bytes_for(int s_pad, int variant, int seg, int &cb)
+{
+    const int row = seg * general_row_bytes_per_sample(variant) + (int)sizeof(ChirpRec);
+    const int tab = seg * general_table_bytes_per_sample(variant);
+    cb = seg >= s_pad ? std::max(1, (kGeneralStageTarget - tab) / row) : 1;
+    return (int)round_up((size_t)cb * row + tab, 128);
+}
+
+int general_segment_samples(int s_pad, int variant)
+{
+    const int per = general_row_bytes_per_sample(variant) + general_table_bytes_per_sample(variant);
+    const int smax = std::max(kSampleAlign, (kGeneralStageTarget - (int)sizeof(ChirpRec)) / per / kSampleAlign *
+                                                kSampleAlign);
+    const int nseg = (s_pad + smax - 1) / smax;
+    return (int)round_up((size_t)((s_pad + nseg - 1) / nseg), kSampleAlign);
+}
+
+int general_seg_len(int s_pad, int variant)
+{
+    const int seg = general_segment_samples(s_pad, variant);
+    if (seg >= s_pad) return s_pad;
+    int cb = 1;
+    const int whole = general_stage_bytes_for(s_pad, variant, s_pad, cb);
+    // 227 KiB of shared memory per CTA, less the kernel's static shared memory
+    if (focus_general_smem_bytes(whole) > 226 * 1024) return seg;
+    const int split = general_stage_bytes_for(s_pad, variant, seg, cb);
+    return focus_general_blocks_per_sm(variant, whole) < focus_general_blocks_per_sm(variant, split) ? seg : s_pad;
 }
 
 // Job record of the resident acquisition x resident grid under the current plan.
@@ -735,7 +773,9 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
                   focus_fp32_seg_blocks_per_sm(seg_stage_bytes);
         }
     }
-    const int stage_bytes = path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, cb)
+    // FP32 general rows likewise: whole, or in segments of about kGeneralStageTarget bytes
+    const int gen_seg = path == TDC_PATH_GENERAL ? general_seg_len(p->s_pad, variant) : 0;
+    const int stage_bytes = path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, gen_seg, cb)
                             : seg                     ? seg_stage_bytes
                                                       : stage_bytes_for(p->s_pad, cb);
     int slots;
@@ -744,7 +784,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
         slots = p->n_sm * bps;
     } else if (path == TDC_PATH_GENERAL) {
-        const int bps = focus_general_blocks_per_sm(variant, stage_bytes, p->s_pad);
+        const int bps = focus_general_blocks_per_sm(variant, stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "general focus kernel does not fit on the device");
         slots = p->n_sm * bps;
     } else {
@@ -790,7 +830,9 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     plan.off_job = L.off_job;
     plan.off_units = L.off_units;
     plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
-    plan.job.seg_len = seg ? kSegmentSamples : 0;
+    plan.job.seg_len = path == TDC_PATH_GENERAL ? gen_seg : seg ? kSegmentSamples : 0;
+    // narrow variants take the phase correction in radians
+    if (path == TDC_PATH_GENERAL && !(variant & 4)) plan.job.gsam = p->gres.as<const float>() + 2 * (size_t)p->s_pad;
     return TDC_OK;
 }
 
@@ -863,8 +905,8 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
                    "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);
-        TDC_CK(launch_focus_general(plan.variant, jobs_dev, units_dev, n_units, counter, status, stage_bytes,
-                                    p->s_pad, grid, st),
+        TDC_CK(launch_focus_general(plan.variant, jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
+                                    st),
                "focus kernel (general)");
     } else {
         TDC_CK(launch_focus_fp64(jobs_dev, units_dev, n_units, status, job.per_sample, st), "focus kernel (fp64)");
@@ -873,6 +915,10 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     launches += 2;
     p->stats.path = path;
     p->stats.correlations = (int64_t)P * C * p->S;
+    const bool staged = path == TDC_PATH_FP32_BULK || path == TDC_PATH_GENERAL;
+    const int row = path == TDC_PATH_GENERAL ? job.seg_len : plan.seg ? kSegmentSamples : p->s_pad;
+    p->stats.stage_samples = staged ? std::min(row, p->s_pad) : 0;
+    p->stats.stage_chirps = staged ? (row < p->s_pad ? 1 : plan.cb) : 0;
     return TDC_OK;
 }
 

@@ -71,6 +71,12 @@ __device__ __forceinline__ float round_small(float v)
 
 // The window-and-residual variant without per-sample positions keeps more samples in
 // flight than 128 registers hold: it runs one CTA per SM instead of spilling.
+//
+// Stages: rows of job.seg_len samples. When a whole row fits (seg_len = s_pad) a stage
+// holds stage_chirps chirps; otherwise each chirp's row is staged in segments, last
+// segment first, and the chirp's Horner state carries from segment to segment. Stage
+// layout: [x rows][trajectory rows][window rows][residual r_s][g_s][records], the
+// per-sample tables only where the variant reads them.
 template <bool TRAJ, bool WIN, bool WIDE>
 __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_MINB)
     focus_general_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
@@ -82,9 +88,6 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
     __shared__ FocusJob sJ;
 
     GenShared &sp = *reinterpret_cast<GenShared *>(smem + kStages * stage_bytes);
-    // per-sample tables of the unit: residual r_s [cycles/m] and g_s (2 pi g_s in the narrow
-    // variants, whose phase correction goes to the sincos in radians)
-    float *const sres = reinterpret_cast<float *>(smem + kStages * stage_bytes + sizeof(GenShared));
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -109,37 +112,69 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
         const int C = sJ.C;
         const int c0 = un.group * sJ.chirps_per_group;
         const int c1 = min(C, c0 + sJ.chirps_per_group);
-        const int CB = sJ.stage_chirps;
-        const int nblk = (c1 - c0 + CB - 1) / CB;
         const int s_pad = sJ.s_pad;
-        float *const sgs = sres + s_pad;
-        const uint32_t xrow = static_cast<uint32_t>(s_pad) * 8u;
-        const uint32_t arow = static_cast<uint32_t>(s_pad) * 16u;
-        // stage layout: [CB x rows][CB trajectory rows][CB window rows][CB records]
+        const int seg = sJ.seg_len;  // samples per staged row segment (multiple of 16)
+        const int nseg = (s_pad + seg - 1) / seg;
+        const int CB = nseg == 1 ? sJ.stage_chirps : 1;
+        const int nblk = nseg == 1 ? (c1 - c0 + CB - 1) / CB : (c1 - c0) * nseg;
+        const uint32_t xrow = static_cast<uint32_t>(seg) * 8u;
+        const uint32_t arow = static_cast<uint32_t>(seg) * 16u;
+        const uint32_t grow = static_cast<uint32_t>(seg) * 4u;
         const uint32_t off_a = CB * xrow;
         const uint32_t off_b = off_a + (TRAJ ? CB * arow : 0u);
-        const uint32_t off_r = off_b + (WIN ? CB * arow : 0u);
+        const uint32_t off_g = off_b + (WIN ? CB * arow : 0u);
+        const uint32_t off_r = off_g + (WIDE ? grow : 0u) + (TRAJ ? grow : 0u);
         const float4 *__restrict__ xw = sJ.xw;
         const float4 *__restrict__ traj = sJ.traj;
         const float4 *__restrict__ wins = sJ.wins;
+        const float *__restrict__ gres = sJ.gres;
+        const float *__restrict__ gsam = sJ.gsam;
         const ChirpRec *__restrict__ chirps = sJ.chirps;
 
+        // stage j -> first chirp, chirps, segment, sample offset, samples
+        auto stage_of = [&](int j, int &cb0, int &cnt, int &sg, int &off, int &len) {
+            if (nseg == 1) {
+                cb0 = c0 + j * CB;
+                cnt = min(CB, c1 - cb0);
+                sg = 0;
+            } else {
+                cb0 = c0 + j / nseg;
+                cnt = 1;
+                sg = nseg - 1 - j % nseg;
+            }
+            off = sg * seg;
+            len = min(seg, s_pad - off);
+        };
+
         auto issue = [&](int j) {
-            const int cb0 = c0 + j * CB;
-            const int cnt = min(CB, c1 - cb0);
+            int cb0, cnt, sg, off, len;
+            stage_of(j, cb0, cnt, sg, off, len);
             const int st = n_issued % kStages;
             unsigned char *base = smem + st * stage_bytes;
-            const uint32_t bx = cnt * xrow, ba = TRAJ ? cnt * arow : 0u, bw = WIN ? cnt * arow : 0u,
-                           br = cnt * (uint32_t)sizeof(ChirpRec);
-            mbar_arrive_expect_tx(&full_bar[st], bx + ba + bw + br);
-            bulk_g2s(base, xw + (size_t)cb0 * (s_pad / 2), bx, &full_bar[st]);
-            if (TRAJ) bulk_g2s(base + off_a, traj + (size_t)cb0 * s_pad, ba, &full_bar[st]);
-            if (WIN) bulk_g2s(base + off_b, wins + (size_t)cb0 * s_pad, bw, &full_bar[st]);
-            bulk_g2s(base + off_r, chirps + cb0, br, &full_bar[st]);
+            const uint32_t lx = static_cast<uint32_t>(len) * 8u, la = static_cast<uint32_t>(len) * 16u,
+                           lg = static_cast<uint32_t>(len) * 4u;
+            uint32_t total = cnt * (lx + (TRAJ ? la : 0u) + (WIN ? la : 0u) + (uint32_t)sizeof(ChirpRec));
+            if (WIDE) total += lg;
+            if (TRAJ) total += lg;
+            mbar_arrive_expect_tx(&full_bar[st], total);
+            for (int cc = 0; cc < cnt; ++cc) {
+                const size_t row = (size_t)(cb0 + cc) * s_pad + off;
+                bulk_g2s(base + cc * xrow, xw + row / 2, lx, &full_bar[st]);
+                if (TRAJ) bulk_g2s(base + off_a + cc * arow, traj + row, la, &full_bar[st]);
+                if (WIN) bulk_g2s(base + off_b + cc * arow, wins + row, la, &full_bar[st]);
+            }
+            uint32_t og = off_g;
+            if (WIDE) {
+                bulk_g2s(base + og, gres + off, lg, &full_bar[st]);
+                og += grow;
+            }
+            if (TRAJ) bulk_g2s(base + og, gsam + off, lg, &full_bar[st]);
+            bulk_g2s(base + off_r, chirps + cb0, cnt * (uint32_t)sizeof(ChirpRec), &full_bar[st]);
             ++n_issued;
         };
 
         if (tid == 0) {
+            fence_proxy_async_smem();
             const int npro = nblk < kStages ? nblk : kStages;
             for (int j = 0; j < npro; ++j) issue(j);
         }
@@ -161,13 +196,6 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
             sp.t[i * 6 + 4][tid] = lo.y;
             sp.t[i * 6 + 5][tid] = lo.z;
         }
-        if (WIDE || TRAJ) {
-            for (int s = tid; s < s_pad; s += kT) {
-                if (WIDE) sres[s] = sJ.gres[s];
-                if (TRAJ) sgs[s] = WIDE ? sJ.gsam[s] : kTwoPiF * sJ.gsam[s];
-            }
-            __syncthreads();
-        }
 
         const float g0h = sJ.g0_hi, g0l = sJ.g0_lo, g1 = sJ.g1, g1l = sJ.g1_lo;
         const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
@@ -175,7 +203,6 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
         const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
         const int chunk = sJ.chunk;
         const SkipPoint *__restrict__ skip = sJ.skip;
-        const int nb = s_pad / kL;
 
         float2 sum[kPT], comp[kPT];
         float wskip[kPT];
@@ -185,6 +212,12 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
             comp[i] = make_float2(0.f, 0.f);
             wskip[i] = 1.0f;
         }
+        // per-(pixel, chirp) state, carried across the segments of a chirp
+        float2 p[kPT][kL - 1];
+        float2 ql[kPT], q0[kPT], h[kPT];
+        float t2x[kPT], t2y[kPT], t2z[kPT];
+        float r0[kPT], a2[kPT], b2[kPT];  // R0, 1/2R0, 1/R0^2
+        bool live = true;
         int cur_chunk = -1;
         bool timed_out = false;
 
@@ -198,97 +231,100 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
             }
             const unsigned char *base = smem + st * stage_bytes;
             const ChirpRec *recs = reinterpret_cast<const ChirpRec *>(base + off_r);
-            const int cb0 = c0 + j * CB;
-            const int cnt = min(CB, c1 - cb0);
+            const float *sgr = reinterpret_cast<const float *>(base + off_g);           // r_s of the segment
+            const float *sgg = sgr + (WIDE ? seg : 0);                                  // g_s of the segment
+            int cb0, cnt, sg, off, len;
+            stage_of(j, cb0, cnt, sg, off, len);
 
             for (int cc = 0; cc < cnt; ++cc) {
                 const int c = cb0 + cc;
-                if (skip_test) {
-                    const int k = c / chunk;
-                    if (k != cur_chunk) {
-                        cur_chunk = k;
-#pragma unroll
-                        for (int i = 0; i < kPT; ++i)
-                            wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, sp.t[i * 6 + 0][tid],
-                                                        sp.t[i * 6 + 1][tid], sp.t[i * 6 + 2][tid], tol, half_bw)
-                                           ? 1.0f
-                                           : 0.0f;
-                    }
-                }
-                const ChirpRec r = recs[cc];
-                const float4 *xs = reinterpret_cast<const float4 *>(base) + (size_t)cc * (s_pad / 2);
-                const float4 *as = reinterpret_cast<const float4 *>(base + off_a) + (size_t)cc * s_pad;
-                const float4 *bs = reinterpret_cast<const float4 *>(base + off_b) + (size_t)cc * s_pad;
+                const float4 *xs = reinterpret_cast<const float4 *>(base) + (size_t)cc * (seg / 2);
+                const float4 *as = reinterpret_cast<const float4 *>(base + off_a) + (size_t)cc * seg;
+                const float4 *bs = reinterpret_cast<const float4 *>(base + off_b) + (size_t)cc * seg;
 
-                float2 p[kPT][kL - 1];
-                float2 ql[kPT], q0[kPT], h[kPT];
-                float t2x[kPT], t2y[kPT], t2z[kPT];
-                float r0[kPT], a2[kPT], b2[kPT];  // R0, 1/2R0, 1/R0^2
-                bool live = false;
+                if (sg == nseg - 1) {
+                    // first staged segment of the chirp: skip weight, range, phase set-up
+                    if (skip_test) {
+                        const int k = c / chunk;
+                        if (k != cur_chunk) {
+                            cur_chunk = k;
 #pragma unroll
-                for (int i = 0; i < kPT; ++i) {
-                    float dxh, dxl, dyh, dyl, dzh, dzl;
-                    dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
-                    dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
-                    dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
-                    float rh, rl, rs, dh;
-                    dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
-                    const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
-                    float bh = g1 * rh;
-                    float bl = fmaf(g1, rh, -bh);
-                    bl = fmaf(g1, rl, bl);
-                    bl = fmaf(g1l, rh, bl);
-                    bh -= rintf(bh);
-                    float s1, c1s;
-                    __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
-                    p[i][0] = make_float2(c1s, s1);
-#pragma unroll
-                    for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
-                    const float lbh = (float)kL * bh;
-                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
-                    float sl, cl;
-                    sincospif(2.0f * lfr, &sl, &cl);
-                    ql[i] = make_float2(cl, sl);
-                    float w = wskip[i];
-                    if (!WIN) {
-                        const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
-                        w *= doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                            for (int i = 0; i < kPT; ++i)
+                                wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, sp.t[i * 6 + 0][tid],
+                                                            sp.t[i * 6 + 1][tid], sp.t[i * 6 + 2][tid], tol,
+                                                            half_bw)
+                                               ? 1.0f
+                                               : 0.0f;
+                        }
                     }
-                    live |= w != 0.0f;
-                    float sa, ca;
-                    __sincosf(kTwoPiF * alpha, &sa, &ca);
-                    q0[i] = make_float2(w * ca, w * sa);
-                    h[i] = make_float2(0.f, 0.f);
-                    // TRAJ: 2 (P0 - T) for the range change; else the unit vector (P0 - T) / R0
-                    // of the per-sample window
-                    const float sc = TRAJ ? 2.0f : rs;
-                    t2x[i] = sc * dxh;
-                    t2y[i] = sc * dyh;
-                    t2z[i] = sc * dzh;
-                    r0[i] = rh;
-                    a2[i] = 0.5f * rs;  // 1 / 2R0
-                    b2[i] = rs * rs;    // 1 / R0^2
+                    const ChirpRec r = recs[cc];
+                    bool any = false;
+#pragma unroll
+                    for (int i = 0; i < kPT; ++i) {
+                        float dxh, dxl, dyh, dyl, dzh, dzl;
+                        dd_sub(r.p_hi.x, r.p_lo.x, sp.t[i * 6 + 0][tid], sp.t[i * 6 + 3][tid], dxh, dxl);
+                        dd_sub(r.p_hi.y, r.p_lo.y, sp.t[i * 6 + 1][tid], sp.t[i * 6 + 4][tid], dyh, dyl);
+                        dd_sub(r.p_hi.z, r.p_lo.z, sp.t[i * 6 + 2][tid], sp.t[i * 6 + 5][tid], dzh, dzl);
+                        float rh, rl, rs, dh;
+                        dd_range(dxh, dxl, dyh, dyl, dzh, dzl, rh, rl, rs, dh);
+                        const float alpha = dd_frac_mul(g0h, g0l, rh, rl);
+                        float bh = g1 * rh;
+                        float bl = fmaf(g1, rh, -bh);
+                        bl = fmaf(g1, rl, bl);
+                        bl = fmaf(g1l, rh, bl);
+                        bh -= rintf(bh);
+                        float s1, c1s;
+                        __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
+                        p[i][0] = make_float2(c1s, s1);
+#pragma unroll
+                        for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
+                        const float lbh = (float)kL * bh;
+                        const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
+                        float sl, cl;
+                        sincospif(2.0f * lfr, &sl, &cl);
+                        ql[i] = make_float2(cl, sl);
+                        float w = wskip[i];
+                        if (!WIN) {
+                            const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                            w *= doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
+                        }
+                        any |= w != 0.0f;
+                        float sa, ca;
+                        __sincosf(kTwoPiF * alpha, &sa, &ca);
+                        q0[i] = make_float2(w * ca, w * sa);
+                        h[i] = make_float2(0.f, 0.f);
+                        // TRAJ: 2 (P0 - T) for the range change; else the unit vector (P0 - T) / R0
+                        // of the per-sample window
+                        const float sc = TRAJ ? 2.0f : rs;
+                        t2x[i] = sc * dxh;
+                        t2y[i] = sc * dyh;
+                        t2z[i] = sc * dzh;
+                        r0[i] = rh;
+                        a2[i] = 0.5f * rs;  // 1 / 2R0
+                        b2[i] = rs * rs;    // 1 / R0^2
+                    }
+                    // a chirp whose chirp-level weight (skip test, and the window unless it is
+                    // per sample) is zero for every pixel of the warp contributes nothing
+                    live = __any_sync(0xffffffffu, any);
                 }
-                // a chirp whose chirp-level weight (skip test, and the window unless it is
-                // per sample) is zero for every pixel of the warp contributes nothing
-                if (!__any_sync(0xffffffffu, live)) continue;
+                if (!live) continue;
 
-                // Horner over blocks, last block first; each sample corrected per pixel.
-                for (int b = nb - 1; b >= 0; --b) {
+                // Horner over this segment's blocks, last block first; each sample corrected per pixel.
+                for (int b = len / kL - 1; b >= 0; --b) {
                     float2 acc[kPT];
 #pragma unroll
                     for (int i = 0; i < kPT; ++i) acc[i] = cmul(h[i], ql[i]);
 #pragma unroll
                     for (int k = 0; k < kL; ++k) {
-                        const int s = b * kL + k;
+                        const int s = b * kL + k;  // sample within the segment
                         const float4 xv = xs[s >> 1];
                         const float xr = (k & 1) ? xv.z : xv.x;
                         const float xi = (k & 1) ? xv.w : xv.y;
                         float4 av = make_float4(0.f, 0.f, 0.f, 0.f), bv = av;
                         if (TRAJ) av = as[s];
                         if (WIN) bv = bs[s];
-                        const float res = WIDE ? sres[s] : 0.0f;
-                        const float gsv = TRAJ ? sgs[s] : 0.0f;
+                        const float res = WIDE ? sgr[s] : 0.0f;
+                        const float gsv = TRAJ ? sgg[s] : 0.0f;
 #pragma unroll
                         for (int i = 0; i < kPT; ++i) {
                             float yr = xr, yi = xi;
@@ -354,15 +390,17 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                     for (int i = 0; i < kPT; ++i) h[i] = acc[i];
                 }
 
+                if (sg == 0) {
 #pragma unroll
-                for (int i = 0; i < kPT; ++i) {
-                    const float2 v = cmul(q0[i], h[i]);
-                    const float yr = v.x - comp[i].x, yi = v.y - comp[i].y;
-                    const float tr = sum[i].x + yr, ti = sum[i].y + yi;
-                    comp[i].x = (tr - sum[i].x) - yr;
-                    comp[i].y = (ti - sum[i].y) - yi;
-                    sum[i].x = tr;
-                    sum[i].y = ti;
+                    for (int i = 0; i < kPT; ++i) {
+                        const float2 v = cmul(q0[i], h[i]);
+                        const float yr = v.x - comp[i].x, yi = v.y - comp[i].y;
+                        const float tr = sum[i].x + yr, ti = sum[i].y + yi;
+                        comp[i].x = (tr - sum[i].x) - yr;
+                        comp[i].y = (ti - sum[i].y) - yi;
+                        sum[i].x = tr;
+                        sum[i].y = ti;
+                    }
                 }
             }
 
@@ -417,16 +455,16 @@ KernelFn select_kernel(int variant)
 
 }  // namespace
 
-int focus_general_smem_bytes(int stage_bytes, int s_pad)
+int focus_general_smem_bytes(int stage_bytes)
 {
-    return kStages * stage_bytes + (int)sizeof(GenShared) + 2 * s_pad * (int)sizeof(float);
+    return kStages * stage_bytes + (int)sizeof(GenShared);
 }
 
-int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad)
+int focus_general_blocks_per_sm(int variant, int stage_bytes)
 {
     KernelFn fn = select_kernel(variant);
     if (!fn) return 0;
-    const int smem = focus_general_smem_bytes(stage_bytes, s_pad);
+    const int smem = focus_general_smem_bytes(stage_bytes);
     if (allow_max_dynamic_smem(fn) != cudaSuccess) return 0;
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kT, smem) != cudaSuccess) return 0;
@@ -434,12 +472,11 @@ int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad)
 }
 
 cudaError_t launch_focus_general(int variant, const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
-                                 int *counter_dev, int *status_dev, int stage_bytes, int s_pad, int grid_ctas,
-                                 cudaStream_t st)
+                                 int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas, cudaStream_t st)
 {
     KernelFn fn = select_kernel(variant);
     if (!fn) return cudaErrorInvalidValue;
-    const int smem = focus_general_smem_bytes(stage_bytes, s_pad);
+    const int smem = focus_general_smem_bytes(stage_bytes);
     cudaError_t e = allow_max_dynamic_smem(fn);
     if (e != cudaSuccess) return e;
     fn<<<grid_ctas, kT, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev, status_dev, stage_bytes);

@@ -69,7 +69,8 @@ struct FocusJob {
     const float4 *wins;      // [C][s_pad] (velocity x -2/(lambda B), window centre / B) per sample (FP32 general
                              // kernel, per-sample windows)
     const float *gres;       // [s_pad] 2 f_s / c0 - (g0 + g1 s) (FP32 general kernel, non-uniform sampling)
-    const float *gsam;       // [s_pad] 2 f_s / c0 [cycles / m] (FP32 general kernel, per-sample positions)
+    const float *gsam;       // [s_pad] 2 f_s / c0 [cycles / m] (wide variants) or 2 pi x that [rad / m]
+                             // (narrow variants) (FP32 general kernel, per-sample positions)
     float4 *partial;         // [n_groups][P]: (sum.re, sum.im, comp.re, comp.im)
     long long P;
     int C;
@@ -89,7 +90,8 @@ struct FocusJob {
     float inv_bw;            // 1 / dopplerBandwidth
     float az_a;              // azimuth window a
     float g1_lo;             // low part of g1 (double-float pair)
-    int seg_len;             // samples per pipeline stage of a chirp staged in segments (0: whole rows)
+    int seg_len;             // samples per pipeline stage of a chirp staged in segments (FP32 bulk: 0 for
+                             // whole rows; FP32 general: s_pad for whole rows)
     int pad_;
 };
 
@@ -139,12 +141,14 @@ cudaError_t launch_focus_reduce(const float4 *partial, int n_groups, long long P
                                 cudaStream_t st);
 // FP32 general focus (tdc_general.cu). variant bits: 1 per-sample positions, 2 per-sample
 // windows, 4 wide (non-uniform sampling residual, large intra-chirp motion: reduced phase
-// correction, longer range-change series); at least one set.
+// correction, longer range-change series); at least one set. Rows are staged job.seg_len
+// samples at a time: whole rows (seg_len = s_pad, job.stage_chirps chirps a stage) or
+// segments of one chirp; stage_bytes = chirps x (seg_len x row bytes per sample + one
+// record) + seg_len x table bytes per sample (see general_stage_bytes_for).
 cudaError_t launch_focus_general(int variant, const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
-                                 int *counter_dev, int *status_dev, int stage_bytes, int s_pad, int grid_ctas,
-                                 cudaStream_t st);
-int focus_general_blocks_per_sm(int variant, int stage_bytes, int s_pad);
-int focus_general_smem_bytes(int stage_bytes, int s_pad);
+                                 int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas, cudaStream_t st);
+int focus_general_blocks_per_sm(int variant, int stage_bytes);
+int focus_general_smem_bytes(int stage_bytes);
 
 // Adjoint of the FP32-bulk focus w.r.t. per-chirp position offsets: per-(tile, chirp)
 // float4 partials, then an FP64 sum over tiles into grad[C][3].

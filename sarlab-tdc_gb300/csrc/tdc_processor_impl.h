@@ -222,7 +222,13 @@ int stage_bytes_for(int s_pad, int &cb);
 // True when a whole row of s_pad samples does not fit the FP32-bulk kernel's stages.
 bool needs_segments(int s_pad);
 // Stage bytes of the FP32 general kernel for a variant (bit 1 per-sample positions, 2 windows).
-int general_stage_bytes_for(int s_pad, int variant, int &cb);
+// FP32 general kernel stages: bytes of a stage of rows staged `seg` samples at a time
+// (seg = s_pad: whole rows, cb chirps a stage; else cb = 1), the samples of a balanced
+// segment, and the staging the focus uses (whole rows unless they do not fit or
+// segments keep more CTAs resident).
+int general_stage_bytes_for(int s_pad, int variant, int seg, int &cb);
+int general_segment_samples(int s_pad, int variant);
+int general_seg_len(int s_pad, int variant);
 // Variant bits of the FP32 general kernel for the resident acquisition.
 int general_variant(const tdc_processor *p);
 FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path);

@@ -485,3 +485,36 @@ def test_long_chirps_are_staged_in_segments(cuda_device, n_samples, band):
     assert stats["path_name"] == "fp32_bulk"
     ref = _oracle(api, sc.grid, args).reshape(img.shape)
     _check(img, ref, l2=2e-4 if np.isfinite(band) else L2_TOL, phase=None if np.isfinite(band) else PHASE_TOL)
+
+
+@pytest.mark.parametrize("case,n_samples", [("traj_win", 6000), ("traj", 9000), ("nonunif", 5000), ("all", 3000)])
+def test_fp32_general_kernel_long_chirps_in_segments(cuda_device, case, n_samples):
+    """Per-sample inputs with rows longer than the general kernel's stages: rows (and the
+    per-sample frequency tables) are staged in segments, last segment first, with each
+    chirp's Horner state carried across them; the FP32 general kernel keeps the job
+    (parity with the FP64 oracle)."""
+    sc = scenes.small_scene(seed=91, n_pri=36, n_samples=n_samples, nx=9, ny=7, rail_len=0.1, device="cuda")
+    traj = "traj" in case or case == "all"
+    win = "win" in case or case == "all"
+    nonunif = "nonunif" in case or case == "all"
+    api = _general_api(sc, traj=traj, win=win, nonunif=nonunif, drift=0.1e-3)
+    args = (0.0, 30.0 if win else INF, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == "general"
+    assert 0 < stats["stage_samples"] < n_samples and stats["stage_chirps"] == 1
+    assert stats["stage_samples"] % 16 == 0
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    if win:
+        _check(img, ref, l2=2e-4, phase=None)
+    else:
+        _check(img, ref)
+
+
+def test_fp32_general_kernel_stages_whole_rows_when_they_fit(cuda_device):
+    """Short per-sample rows are staged whole, several chirps a stage."""
+    sc = scenes.small_scene(seed=92, n_pri=64, n_samples=64, nx=8, ny=8, device="cuda")
+    api = _general_api(sc, traj=True)
+    img, stats, _ = run_engine(api, sc.grid, (0.0, INF, False, True, True))
+    assert stats["path_name"] == "general"
+    assert stats["stage_samples"] == 64 and stats["stage_chirps"] > 1
+    _check(img, _oracle(api, sc.grid, (0.0, INF, False, True, True)).reshape(img.shape))
