@@ -136,6 +136,9 @@ typedef struct tdc_start_stats {
     int stage_samples;    /* samples of a chirp row per pipeline stage of the FP32 kernels
                              (the whole row, or one segment of a long row; 0 on FP64 paths) */
     int stage_chirps;     /* chirp rows per pipeline stage (1 when rows are staged in segments) */
+    int general_variant;  /* FP32 general kernel variant bits (1 per-sample positions, 2 per-sample
+                             windows, 4 wide phase correction); 0 on the other paths */
+    int reserved;
 } tdc_start_stats;
 
 typedef enum tdc_path {

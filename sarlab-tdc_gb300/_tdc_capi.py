@@ -120,6 +120,8 @@ class StartStats(C.Structure):
         ("kernel_launches", C.c_int),
         ("stage_samples", C.c_int),
         ("stage_chirps", C.c_int),
+        ("general_variant", C.c_int),
+        ("reserved", C.c_int),
     ]
 
     def as_dict(self) -> dict:

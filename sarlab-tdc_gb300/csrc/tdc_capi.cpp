@@ -86,7 +86,14 @@ constexpr double kUniformPhaseTolRad = 1e-4;
 constexpr double kGeneralMaxEps = 0.1;
 constexpr double kGeneralNarrowEps = 0.02;
 constexpr double kGeneralNarrowCycles = 4.0;
-constexpr int kGeneralStageTarget = 32768;
+#ifndef TDC_GENERAL_STAGE_TARGET
+#define TDC_GENERAL_STAGE_TARGET 32768
+#endif
+// 1: stage general-kernel rows in segments whenever a row exceeds the stage target (tuning)
+#ifndef TDC_GENERAL_ALWAYS_SEGMENT
+#define TDC_GENERAL_ALWAYS_SEGMENT 0
+#endif
+constexpr int kGeneralStageTarget = TDC_GENERAL_STAGE_TARGET;
 // Long chirps: samples per staged segment when a whole row does not fit the bulk kernel's stages.
 constexpr int kSegmentSamples = 2048;
 
@@ -589,27 +596,33 @@ int choose_path(const tdc_processor *p)
     return TDC_PATH_GENERAL;
 }
 
-// Split the chirps into groups so that tiles x groups units fill whole waves of `slots`.
-void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg)
+// Split the chirps into groups so that tiles x groups units fill whole waves of `slots`;
+// among the splits with at least min_units_per_slot units per slot when there are any.
+void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot)
 {
     const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
-    double best = std::numeric_limits<double>::infinity();
+    const long long min_units = (long long)min_units_per_slot * slots;
+    const int gmax = std::max(1, std::min(C, 1024));
     n_groups = 1;
     cpg = C;
-    const int gmax = std::max(1, std::min(C, 1024));
-    for (int g = 1; g <= gmax; ++g) {
-        const int c = (C + g - 1) / g;
-        const int geff = (C + c - 1) / c;
-        if (geff != g) continue;
-        const long long units = n_tiles * geff;
-        if (units > (1LL << 24)) break;
-        const long long waves = (units + slots - 1) / slots;
-        const double cost = (double)waves * (c + 0.5);
-        if (cost < best - 1e-9) {
-            best = cost;
-            n_groups = geff;
-            cpg = c;
+    for (int pass = 0; pass < 2; ++pass) {
+        double best = std::numeric_limits<double>::infinity();
+        for (int g = 1; g <= gmax; ++g) {
+            const int c = (C + g - 1) / g;
+            const int geff = (C + c - 1) / c;
+            if (geff != g) continue;
+            const long long units = n_tiles * geff;
+            if (units > (1LL << 24)) break;
+            if (pass == 0 && units < min_units) continue;
+            const long long waves = (units + slots - 1) / slots;
+            const double cost = (double)waves * (c + 0.5);
+            if (cost < best - 1e-9) {
+                best = cost;
+                n_groups = geff;
+                cpg = c;
+            }
         }
+        if (best < std::numeric_limits<double>::infinity()) return;
     }
 }
 
@@ -680,6 +693,7 @@ int general_seg_len(int s_pad, int variant)
 {
     const int seg = general_segment_samples(s_pad, variant);
     if (seg >= s_pad) return s_pad;
+    if (TDC_GENERAL_ALWAYS_SEGMENT) return seg;
     int cb = 1;
     const int whole = general_stage_bytes_for(s_pad, variant, s_pad, cb);
     // 227 KiB of shared memory per CTA, less the kernel's static shared memory
@@ -793,7 +807,8 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 
     if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
         max_unit_work != p->plan_unit_cap) {
-        plan_groups(P, C, slots, p->plan_groups, p->plan_cpg);
+        plan_groups(P, C, slots, p->plan_groups, p->plan_cpg,
+                    path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot);
         if (max_unit_work > 0) {
             // bound the work of one unit (tile x chirp group): at most cap / (tile x S) chirps per group
             const int cpg_cap = std::max(1, (int)(max_unit_work / ((double)kFocusTile * p->S)));
@@ -919,6 +934,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     const int row = path == TDC_PATH_GENERAL ? job.seg_len : plan.seg ? kSegmentSamples : p->s_pad;
     p->stats.stage_samples = staged ? std::min(row, p->s_pad) : 0;
     p->stats.stage_chirps = staged ? (row < p->s_pad ? 1 : plan.cb) : 0;
+    p->stats.general_variant = path == TDC_PATH_GENERAL ? plan.variant : 0;
     return TDC_OK;
 }
 
@@ -1294,7 +1310,7 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     if (bps <= 0) return fail(TDC_ERR_CUDA, "adjoint kernel does not fit on the device");
     const int slots = p->n_sm * bps;
     int n_groups = 1, cpg = C;
-    plan_groups(P, C, slots, n_groups, cpg);
+    plan_groups(P, C, slots, n_groups, cpg, kFocusMinUnitsPerSlot);
     const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
     std::vector<FocusUnit> units;
     units.reserve((size_t)(n_tiles * n_groups));

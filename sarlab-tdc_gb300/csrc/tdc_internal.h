@@ -28,6 +28,19 @@ constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows
 #define TDC_FOCUS_STAGE_TARGET 16640
 #endif
 constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp rows + records per pipeline stage
+// Fewest work units per CTA slot the planner aims for where the grid and chirps allow
+// it. CTAs that share an SM need not progress at the same rate, so with a few long
+// units per slot the last units end far apart (measured on 256^2 pixels x 256 chirps
+// x 1024 samples, general kernel: SMs busy 72-100% of the launch at 3 units per slot,
+// +14% throughput at 4 or more).
+#ifndef TDC_GENERAL_MIN_UNITS
+#define TDC_GENERAL_MIN_UNITS 4
+#endif
+#ifndef TDC_FOCUS_MIN_UNITS
+#define TDC_FOCUS_MIN_UNITS 8
+#endif
+constexpr int kGeneralMinUnitsPerSlot = TDC_GENERAL_MIN_UNITS;
+constexpr int kFocusMinUnitsPerSlot = TDC_FOCUS_MIN_UNITS;
 // Pixels per thread of the FP32 general kernel (per-sample trajectories / windows, non-uniform sampling).
 #ifndef TDC_GENERAL_PT
 #define TDC_GENERAL_PT 2

@@ -217,7 +217,7 @@ struct FocusPlan {
 int prepare(tdc_processor *p, const StartOpts &o, int &launches);
 int upload_grid(tdc_processor *p, int &launches);
 int choose_path(const tdc_processor *p);
-void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg);
+void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot);
 int stage_bytes_for(int s_pad, int &cb);
 // True when a whole row of s_pad samples does not fit the FP32-bulk kernel's stages.
 bool needs_segments(int s_pad);

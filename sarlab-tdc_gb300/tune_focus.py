@@ -9,12 +9,15 @@ synthetic shapes with the acquisition and grid resident on the device:
     3: 1024^2 pixels x 4096 chirps x  256 samples (the 3-D volume's sample count)
     1: 256^2 pixels x 1024 chirps x 512 samples (the small stripmap case)
 
-and, for the general kernel (TDC_GENERAL_PT, TDC_GENERAL_MINB), on 512^2 pixels x
-1024 chirps x 1024 samples with FP32 per-sample inputs:
+and, for the general kernel (TDC_GENERAL_PT, TDC_GENERAL_MINB, TDC_GENERAL_STAGE_TARGET,
+TDC_GENERAL_ALWAYS_SEGMENT),
+on 512^2 pixels x 1024 chirps x 1024 samples with FP32 per-sample inputs:
 
     g:  positions drifting ~0.3 mm within each chirp
     gw: the same plus per-sample velocity under a 30 Hz Doppler band
     gn: jittered (non-uniform) sample times
+    gl: positions as g on long chirps, 256^2 pixels x 256 chirps x 4096 samples (rows
+        staged in segments)
 
 Timing: 2 warm-up focuses, then the mean of 3 focuses between CUDA events on the
 launching stream. Each variant's image is compared with the first variant's.
@@ -46,6 +49,8 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     band = float("inf")
     if shape == "1":
         sc = scenes.config1(device="cuda")
+    elif shape == "gl":
+        sc = scenes.config2(device="cuda", n_pix_side=256, n_pri=256, n_samples=4096, n_targets=8)
     elif shape.startswith("g"):
         sc = scenes.config2(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
     else:
@@ -56,7 +61,7 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     if shape.startswith("g"):
         C, S = sc.n_pri, sc.n_samples
         rng = np.random.default_rng(1)
-        if shape in ("g", "gw"):
+        if shape in ("g", "gw", "gl"):
             pos = np.broadcast_to(sc.positions[:, None, :], (C, S, 3)) + \
                 (np.arange(S) / S)[None, :, None] * rng.normal(0.0, 0.3e-3, (C, 1, 3))
             api["position"] = np.ascontiguousarray(pos, dtype=np.float32)
@@ -95,7 +100,9 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     if not ref_f.exists():
         np.save(ref_f, out)
     ref = np.load(ref_f)
+    st = p.lastStats()
     return {"ms": round(ms, 3), "gcorr_s": round(sc.correlations() / (ms / 1e3) / 1e9, 1), "path": p.path(),
+            "stage": [st["stage_samples"], st["stage_chirps"]],
             "rel_vs_first": float(np.linalg.norm(out - ref) / np.linalg.norm(ref))}
 
 
