@@ -18,6 +18,7 @@ on 512^2 pixels x 1024 chirps x 1024 samples with FP32 per-sample inputs:
     gn: jittered (non-uniform) sample times
     gl: positions as g on long chirps, 256^2 pixels x 256 chirps x 4096 samples (rows
         staged in segments)
+    gs: positions as g on a small aperture, 256^2 pixels x 256 chirps x 1024 samples
 
 Timing: 2 warm-up focuses, then the mean of 3 focuses between CUDA events on the
 launching stream. Each variant's image is compared with the first variant's.
@@ -49,8 +50,9 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     band = float("inf")
     if shape == "1":
         sc = scenes.config1(device="cuda")
-    elif shape == "gl":
-        sc = scenes.config2(device="cuda", n_pix_side=256, n_pri=256, n_samples=4096, n_targets=8)
+    elif shape in ("gl", "gs"):
+        sc = scenes.config2(device="cuda", n_pix_side=256, n_pri=256, n_samples=4096 if shape == "gl" else 1024,
+                            n_targets=8)
     elif shape.startswith("g"):
         sc = scenes.config2(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
     else:
@@ -61,7 +63,7 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     if shape.startswith("g"):
         C, S = sc.n_pri, sc.n_samples
         rng = np.random.default_rng(1)
-        if shape in ("g", "gw", "gl"):
+        if shape in ("g", "gw", "gl", "gs"):
             pos = np.broadcast_to(sc.positions[:, None, :], (C, S, 3)) + \
                 (np.arange(S) / S)[None, :, None] * rng.normal(0.0, 0.3e-3, (C, 1, 3))
             api["position"] = np.ascontiguousarray(pos, dtype=np.float32)
