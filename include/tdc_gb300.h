@@ -335,8 +335,14 @@ int tdc_selftest_wait_timeout(int device, int limit_us, int *timed_out, double *
  * (other streams, other host threads) race on it and must be serialised by the
  * caller. The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture. Each call is blocking: it returns after the image is
- * written and the kernels' status word has been read.
+ * any stream capture. tdc_focus_noalloc is blocking: it returns after the image
+ * is written and the kernels' status word has been read (TDC_ERR_TIMEOUT when a
+ * bounded wait in the focus kernel expired). tdc_focus_noalloc_async enqueues the
+ * same kernels and a copy of the status word into status_dev (a device int,
+ * 0 = success, 1 = a bounded wait expired) and returns without synchronising,
+ * so it can be captured into a CUDA graph: the job record is a kernel argument
+ * and the scratch is reset by the captured set-up kernel, so a replay focuses
+ * whatever the input buffers hold at that time.
  *
  * Inputs (device pointers, 16-byte aligned):
  *   samples      n_pri rows of s_pad complex floats (interleaved): the range-
@@ -371,6 +377,7 @@ typedef struct tdc_noalloc_focus_args {
 } tdc_noalloc_focus_args;
 
 int tdc_focus_noalloc(const tdc_noalloc_focus_args *args, float *image_dev, void *stream);
+int tdc_focus_noalloc_async(const tdc_noalloc_focus_args *args, float *image_dev, int *status_dev, void *stream);
 
 #ifdef __cplusplus
 }

@@ -164,6 +164,7 @@ SIGNATURES = [
     ("tdc_probe_fma", C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.POINTER(C.c_double), _vp]),
     ("tdc_selftest_wait_timeout", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("tdc_focus_noalloc", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp]),
+    ("tdc_focus_noalloc_async", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp, _vp]),
     ("tdc_processor_set_chirp_offsets_device", C.c_int, [_vp, _vp, _vp]),
     ("tdc_processor_adjoint_device", C.c_int, [_vp, _vp, _vp, _vp]),
     ("tdc_server_create", C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(_vp)]),

@@ -71,36 +71,40 @@ void split_dd(double v, float &h, float &l)
     l = static_cast<float>(v - static_cast<double>(h));
 }
 
-// Chirp groups so that tiles x groups fill whole waves of `slots`, limited to
+// Chirp groups so that tiles x groups fill whole waves of `slots` (among the splits
+// with at least kFocusMinUnitsPerSlot units per slot when there are any), limited to
 // what fits in the scratch array.
 bool plan(long long P, int C, int slots, int &n_groups, int &cpg, size_t &off_partial)
 {
     const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
-    double best = std::numeric_limits<double>::infinity();
-    bool found = false;
+    const long long min_units = (long long)kFocusMinUnitsPerSlot * slots;
     const int gmax = std::max(1, std::min(C, 1024));
-    for (int g = 1; g <= gmax; ++g) {
-        const int c = (C + g - 1) / g;
-        const int geff = (C + c - 1) / c;
-        if (geff != g) continue;
-        size_t off;
-        if (layout_bytes(P, n_tiles * geff, geff, off) > TDC_NOALLOC_SCRATCH_BYTES) break;
-        const long long waves = (n_tiles * geff + slots - 1) / slots;
-        const double cost = (double)waves * (c + 0.5);
-        if (cost < best - 1e-9) {
-            best = cost;
-            n_groups = geff;
-            cpg = c;
-            off_partial = off;
-            found = true;
+    for (int pass = 0; pass < 2; ++pass) {
+        double best = std::numeric_limits<double>::infinity();
+        for (int g = 1; g <= gmax; ++g) {
+            const int c = (C + g - 1) / g;
+            const int geff = (C + c - 1) / c;
+            if (geff != g) continue;
+            size_t off;
+            if (layout_bytes(P, n_tiles * geff, geff, off) > TDC_NOALLOC_SCRATCH_BYTES) break;
+            if (pass == 0 && n_tiles * geff < min_units) continue;
+            const long long waves = (n_tiles * geff + slots - 1) / slots;
+            const double cost = (double)waves * (c + 0.5);
+            if (cost < best - 1e-9) {
+                best = cost;
+                n_groups = geff;
+                cpg = c;
+                off_partial = off;
+            }
         }
+        if (best < std::numeric_limits<double>::infinity()) return true;
     }
-    return found;
+    return false;
 }
 
-}  // namespace
-
-extern "C" int tdc_focus_noalloc(const tdc_noalloc_focus_args *a, float *image_dev, void *stream)
+// Checks, plans and enqueues the setup, focus and reduce kernels on `st`; nothing
+// blocks. `status_word` receives the device address of the kernels' status word.
+int enqueue(const tdc_noalloc_focus_args *a, float *image_dev, cudaStream_t st, int **status_word)
 {
     // ---- argument and size checks first: nothing below runs for rejected sizes ----
     if (!a || !image_dev) return fail(TDC_ERR_INVALID_ARGUMENT, "null argument");
@@ -188,7 +192,6 @@ extern "C" int tdc_focus_noalloc(const tdc_noalloc_focus_args *a, float *image_d
     job.inv_bw = 1.0f / a->doppler_bandwidth;
     job.az_a = kAzimuthA;
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long long n_units = n_tiles * n_groups;
     const int setup_blocks = (int)std::min<long long>((n_units + 255) / 256, 1024);
     noalloc_setup_kernel<<<setup_blocks, 256, 0, st>>>(job, (int)n_tiles, n_groups, base);
@@ -202,12 +205,36 @@ extern "C" int tdc_focus_noalloc(const tdc_noalloc_focus_args *a, float *image_d
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("focus kernel: ") + cudaGetErrorString(e));
     e = launch_focus_reduce(job.partial, n_groups, P, reinterpret_cast<float2 *>(image_dev), st);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("reduce kernel: ") + cudaGetErrorString(e));
+    *status_word = reinterpret_cast<int *>(base + kOffStatus) + 1;
+    return TDC_OK;
+}
 
-    // Blocking: collect the kernel's status word before returning.
+}  // namespace
+
+extern "C" int tdc_focus_noalloc(const tdc_noalloc_focus_args *a, float *image_dev, void *stream)
+{
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int *status_word = nullptr;
+    if (int rc = enqueue(a, image_dev, st, &status_word)) return rc;
+    // Blocking: collect the kernels' status word before returning.
     int status = 0;
-    e = cudaMemcpyAsync(&status, base + kOffStatus + sizeof(int), sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaMemcpyAsync(&status, status_word, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("focus: ") + cudaGetErrorString(e));
     if (status & kStatusTimeout) return fail(TDC_ERR_TIMEOUT, "focus kernel wait timed out");
+    return TDC_OK;
+}
+
+extern "C" int tdc_focus_noalloc_async(const tdc_noalloc_focus_args *a, float *image_dev, int *status_dev,
+                                       void *stream)
+{
+    if (!status_dev) return fail(TDC_ERR_INVALID_ARGUMENT, "null status word");
+    if (reinterpret_cast<uintptr_t>(status_dev) & 3u)
+        return fail(TDC_ERR_INVALID_ARGUMENT, "status word must be 4-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int *status_word = nullptr;
+    if (int rc = enqueue(a, image_dev, st, &status_word)) return rc;
+    const cudaError_t e = cudaMemcpyAsync(status_dev, status_word, sizeof(int), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("status copy: ") + cudaGetErrorString(e));
     return TDC_OK;
 }

@@ -106,6 +106,81 @@ def test_noalloc_focus_matches_device_focus_twice_in_a_row(cuda_device):
     np.testing.assert_array_equal(outs[0], outs[1])
 
 
+@pytest.mark.gpu
+def test_noalloc_async_captured_in_a_cuda_graph(cuda_device):
+    """tdc_focus_noalloc_async captured into a CUDA graph: a replay gives the blocking
+    call's image bit for bit, and a replay after the caller rewrites the inputs in place
+    focuses the new data (samples doubled: image exactly doubled); the status word the
+    graph copies out reads 0."""
+    import torch
+
+    import _tdc_capi
+    from sarlabtdc import scenes
+
+    lib = _tdc_capi.lib()
+    sc = scenes.small_scene(seed=62, n_pri=256, n_samples=128, nx=40, ny=30, device="cuda")
+    api = sc.api_arrays()
+    samples, chirps, grid_hi, g0, g1, lam = _device_inputs(api, sc.grid, torch)
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = samples.data_ptr()
+    a.chirps = chirps.data_ptr()
+    a.skip_points = None
+    a.grid_hi = grid_hi.data_ptr()
+    a.grid_lo = None
+    a.n_pix = grid_hi.shape[0]
+    a.n_pri = sc.n_pri
+    a.n_samples = sc.n_samples
+    a.g0, a.g1 = g0, g1
+    a.lambda_ = lam
+    a.doppler_bandwidth = float("inf")
+    a.doppler_win_taper = 1
+    n_pix = grid_hi.shape[0]
+    ref = torch.empty(n_pix, dtype=torch.complex64, device="cuda")
+    # the first call on the device (scratch address look-up) runs before any capture
+    rc = lib.tdc_focus_noalloc(C.byref(a), C.c_void_p(ref.data_ptr()),
+                               C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, _tdc_capi.last_error()
+    ref_np = ref.cpu().numpy()
+    assert np.all(np.isfinite(ref_np)) and np.abs(ref_np).max() > 0
+
+    out = torch.full((n_pix,), complex(float("nan"), 0.0), dtype=torch.complex64, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rc = lib.tdc_focus_noalloc_async(C.byref(a), C.c_void_p(out.data_ptr()), C.c_void_p(status.data_ptr()),
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, _tdc_capi.last_error()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), ref_np)
+
+    samples.mul_(2.0)
+    status.fill_(-1)
+    out.fill_(complex(float("nan"), 0.0))
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), 2 * ref_np)
+
+
+def test_noalloc_async_rejects_a_missing_status_word():
+    """Argument check only: returns before any CUDA call."""
+    import _tdc_capi
+
+    lib = _tdc_capi.lib()
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = a.chirps = a.grid_hi = 4096      # never dereferenced
+    a.n_pix = 512
+    a.n_pri = 128
+    a.n_samples = 256
+    a.lambda_ = 0.0039
+    a.doppler_bandwidth = float("inf")
+    rc = lib.tdc_focus_noalloc_async(C.byref(a), C.c_void_p(4096), None, None)
+    assert rc == _tdc_capi.TDC_ERR_INVALID_ARGUMENT
+    assert "status word" in _tdc_capi.last_error()
+
+
 def test_noalloc_rejects_grids_beyond_its_fixed_scratch():
     """Size check only: returns before any CUDA call (run where no GPU is present)."""
     import torch
