@@ -147,8 +147,7 @@ typedef enum tdc_path {
     TDC_PATH_GENERAL = 2,      /* per-sample trajectory / window or non-uniform sample times: FP32 phasors
                                   with a double-float range at sample 0 and per-sample corrections */
     TDC_PATH_GENERAL_FP64 = 3  /* the same inputs with FP64 phase per sample (FP64 precision, or intra-chirp
-                                  motion too large for the FP32 correction, or general-path rows too long to
-                                  stage) */
+                                  motion too large for the FP32 correction) */
 } tdc_path;
 
 int tdc_processor_last_stats(const tdc_processor *proc, tdc_start_stats *out);
