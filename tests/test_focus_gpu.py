@@ -518,3 +518,35 @@ def test_fp32_general_kernel_stages_whole_rows_when_they_fit(cuda_device):
     assert stats["path_name"] == "general"
     assert stats["stage_samples"] == 64 and stats["stage_chirps"] > 1
     _check(img, _oracle(api, sc.grid, (0.0, INF, False, True, True)).reshape(img.shape))
+
+
+@pytest.mark.parametrize("n_pri,n_samples,nx,ny", [(1, 1, 1, 1), (1, 64, 3, 5), (2, 3, 17, 31), (129, 17, 23, 23),
+                                                   (127, 16, 32, 16), (257, 5, 1, 600)])
+def test_parity_ragged_shapes(cuda_device, n_pri, n_samples, nx, ny):
+    """Ragged acquisitions: one chirp, one sample, one pixel, chirp counts either side of
+    the 128-chirp skip chunk, pixel counts either side of the 512-pixel tile; an unbounded
+    band and a finite one (per-chirp windows, skip test on partial chunks) on the FP32-bulk
+    kernel, and positions moving within the chirps on the FP32 general kernel."""
+    sc = scenes.small_scene(seed=100 + n_pri + n_samples, n_pri=n_pri, n_samples=n_samples, nx=nx, ny=ny,
+                            device="cuda")
+    cases = [(_scene_api(sc), (0.0, INF, False, True, True), "fp32_bulk"),
+             (_moving_api(sc, speed=0.08), (2.0, 18.0, False, True, True), "fp32_bulk")]
+    if n_samples > 1:
+        cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "general"))
+    rng = np.random.default_rng(n_pri + n_samples)
+    for api, args, path in cases:
+        if not np.any(api["rawData"]):
+            # a one-sample chirp simulated under a Hann taper is all zero: use seeded noise
+            raw = rng.normal(size=(n_pri, n_samples, 2)).astype(np.float32)
+            api["rawData"] = np.ascontiguousarray(raw[..., 0] + 1j * raw[..., 1]).astype(np.complex64)
+        img, stats, _ = run_engine(api, sc.grid, args)
+        assert img.shape == (ny, nx)
+        assert stats["path_name"] == path
+        ref = _oracle(api, sc.grid, args).reshape(img.shape)
+        assert np.all(np.isfinite(img))
+        if not np.any(ref):
+            assert not np.any(img)  # every chirp windowed out: the reference's image is all zero
+        elif np.isfinite(args[1]):
+            _check(img, ref, l2=2e-4, phase=None)
+        else:
+            _check(img, ref)
