@@ -322,6 +322,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         gres[2 * (size_t)s_pad + s] = (float)(2.0 * M_PI * gsv);
     }
     std::vector<float4> traj, wins;
+    std::vector<float> wdot;
     p->traj_varies = pos_differ;
     p->delta_max = 0.0;
     bool any_velocity = false;
@@ -353,15 +354,22 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     }
     if (p->win_varies) {
         // In band units: velocity x (-2 / lambda) / B and window centre / B, so the kernel forms
-        // (fDop - centre) / B with one dot product and one fused multiply-add.
+        // (fDop - centre) / B with one dot product and one fused multiply-add. With positions
+        // moving within chirps the kernel dots the velocity with 2 (P0 - T) and adds the
+        // pixel-independent part u . D_s from its own table, so u is stored halved.
+        const bool with_traj = p->traj_varies;
         wins.assign((size_t)C * s_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+        if (with_traj) wdot.assign((size_t)C * s_pad, 0.f);
         const double vs = -2.0 / (double)p->lambda / (double)o.bw, cs = 1.0 / (double)o.bw;
+        const double us = with_traj ? 0.5 : 1.0;
         parallel_chirps(C, S, [&](int, int cb, int ce) {
             for (int c = cb; c < ce; ++c)
                 for (int s = 0; s < S; ++s) {
+                    const size_t i = (size_t)c * s_pad + s;
                     const ChirpRec r = make_record(p, c, s, o.centroid != 0, o.center);
-                    wins[(size_t)c * s_pad + s] = make_float4((float)(r.vel.x * vs), (float)(r.vel.y * vs),
-                                                              (float)(r.vel.z * vs), (float)(r.p_hi.w * cs));
+                    const double ux = r.vel.x * vs, uy = r.vel.y * vs, uz = r.vel.z * vs;
+                    wins[i] = make_float4((float)(us * ux), (float)(us * uy), (float)(us * uz), (float)(r.p_hi.w * cs));
+                    if (with_traj) wdot[i] = (float)(ux * traj[i].x + uy * traj[i].y + uz * traj[i].z);
                 }
         });
     }
@@ -462,7 +470,13 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         TDC_CK(cudaMemcpyAsync(p->wins.p, wins.data(), wins.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
                "copy per-sample windows");
     }
-    p->stats.h2d_bytes += (int64_t)gres.size() * 4 + (int64_t)((traj.size() + wins.size()) * sizeof(float4));
+    if (!wdot.empty()) {
+        TDC_CK(p->wdot.ensure(wdot.size() * sizeof(float)), "alloc per-sample window offsets");
+        TDC_CK(cudaMemcpyAsync(p->wdot.p, wdot.data(), wdot.size() * sizeof(float), cudaMemcpyHostToDevice, st),
+               "copy per-sample window offsets");
+    }
+    p->stats.h2d_bytes += (int64_t)(gres.size() + wdot.size()) * 4 +
+                          (int64_t)((traj.size() + wins.size()) * sizeof(float4));
     p->stats.h2d_bytes += (int64_t)C * S * 8 + (int64_t)C * sizeof(ChirpRec) +
                           (int64_t)skip.size() * sizeof(SkipPoint) + (int64_t)S * 8 + (int64_t)C * 24;
     TDC_CK(cudaEventRecord(p->ev[1], st), "event");
@@ -657,10 +671,10 @@ bool needs_segments(int s_pad)
 namespace {
 
 // Bytes the FP32 general kernel stages per (chirp, sample): the raw sample, and the
-// trajectory and window table entries where the variant reads them.
+// trajectory, window and window-offset table entries where the variant reads them.
 int general_row_bytes_per_sample(int variant)
 {
-    return 8 + ((variant & 1) ? 16 : 0) + ((variant & 2) ? 16 : 0);
+    return 8 + ((variant & 1) ? 16 : 0) + ((variant & 2) ? 16 : 0) + ((variant & 3) == 3 ? 4 : 0);
 }
 
 // Bytes of the per-sample frequency tables staged with each row segment: the non-uniform
@@ -713,6 +727,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     job.chirps = p->per_chirp || rec_per_sample ? p->chirps.as<const ChirpRec>() : p->gen_rec.as<const ChirpRec>();
     job.traj = p->traj_varies ? p->traj.as<const float4>() : nullptr;
     job.wins = p->win_varies ? p->wins.as<const float4>() : nullptr;
+    job.wdot = p->win_varies && p->traj_varies ? p->wdot.as<const float>() : nullptr;
     job.gres = p->gres.as<const float>();
     job.gsam = p->gres.as<const float>() + p->s_pad;
     job.grid_hi = p->grid_hi.as<const float4>();

@@ -75,8 +75,8 @@ __device__ __forceinline__ float round_small(float v)
 // Stages: rows of job.seg_len samples. When a whole row fits (seg_len = s_pad) a stage
 // holds stage_chirps chirps; otherwise each chirp's row is staged in segments, last
 // segment first, and the chirp's Horner state carries from segment to segment. Stage
-// layout: [x rows][trajectory rows][window rows][residual r_s][g_s][records], the
-// per-sample tables only where the variant reads them.
+// layout: [x rows][trajectory rows][window rows][window-offset rows][residual r_s][g_s]
+// [records], the per-sample tables only where the variant reads them.
 template <bool TRAJ, bool WIN, bool WIDE>
 __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_MINB)
     focus_general_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
@@ -89,6 +89,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
 
     GenShared &sp = *reinterpret_cast<GenShared *>(smem + kStages * stage_bytes);
 
+    constexpr bool TW = TRAJ && WIN;  // per-sample positions and windows: window-offset rows staged
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int i = 0; i < kStages; ++i) mbar_init(&full_bar[i], 1);
@@ -122,11 +123,13 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
         const uint32_t grow = static_cast<uint32_t>(seg) * 4u;
         const uint32_t off_a = CB * xrow;
         const uint32_t off_b = off_a + (TRAJ ? CB * arow : 0u);
-        const uint32_t off_g = off_b + (WIN ? CB * arow : 0u);
+        const uint32_t off_w = off_b + (WIN ? CB * arow : 0u);
+        const uint32_t off_g = off_w + (TW ? CB * grow : 0u);
         const uint32_t off_r = off_g + (WIDE ? grow : 0u) + (TRAJ ? grow : 0u);
         const float4 *__restrict__ xw = sJ.xw;
         const float4 *__restrict__ traj = sJ.traj;
         const float4 *__restrict__ wins = sJ.wins;
+        const float *__restrict__ wdot = sJ.wdot;
         const float *__restrict__ gres = sJ.gres;
         const float *__restrict__ gsam = sJ.gsam;
         const ChirpRec *__restrict__ chirps = sJ.chirps;
@@ -153,7 +156,8 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
             unsigned char *base = smem + st * stage_bytes;
             const uint32_t lx = static_cast<uint32_t>(len) * 8u, la = static_cast<uint32_t>(len) * 16u,
                            lg = static_cast<uint32_t>(len) * 4u;
-            uint32_t total = cnt * (lx + (TRAJ ? la : 0u) + (WIN ? la : 0u) + (uint32_t)sizeof(ChirpRec));
+            uint32_t total =
+                cnt * (lx + (TRAJ ? la : 0u) + (WIN ? la : 0u) + (TW ? lg : 0u) + (uint32_t)sizeof(ChirpRec));
             if (WIDE) total += lg;
             if (TRAJ) total += lg;
             mbar_arrive_expect_tx(&full_bar[st], total);
@@ -162,6 +166,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                 bulk_g2s(base + cc * xrow, xw + row / 2, lx, &full_bar[st]);
                 if (TRAJ) bulk_g2s(base + off_a + cc * arow, traj + row, la, &full_bar[st]);
                 if (WIN) bulk_g2s(base + off_b + cc * arow, wins + row, la, &full_bar[st]);
+                if (TW) bulk_g2s(base + off_w + cc * grow, wdot + row, lg, &full_bar[st]);
             }
             uint32_t og = off_g;
             if (WIDE) {
@@ -217,6 +222,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
         float2 ql[kPT], q0[kPT], h[kPT];
         float t2x[kPT], t2y[kPT], t2z[kPT];
         float r0[kPT], a2[kPT], b2[kPT];  // R0, 1/2R0, 1/R0^2
+        float r0sq[kPT];                   // R0^2 (per-sample positions and windows)
         bool live = true;
         int cur_chunk = -1;
         bool timed_out = false;
@@ -241,6 +247,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                 const float4 *xs = reinterpret_cast<const float4 *>(base) + (size_t)cc * (seg / 2);
                 const float4 *as = reinterpret_cast<const float4 *>(base + off_a) + (size_t)cc * seg;
                 const float4 *bs = reinterpret_cast<const float4 *>(base + off_b) + (size_t)cc * seg;
+                const float *us = reinterpret_cast<const float *>(base + off_w) + (size_t)cc * seg;
 
                 if (sg == nseg - 1) {
                     // first staged segment of the chirp: skip weight, range, phase set-up
@@ -302,6 +309,7 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                         r0[i] = rh;
                         a2[i] = 0.5f * rs;  // 1 / 2R0
                         b2[i] = rs * rs;    // 1 / R0^2
+                        if (TW) r0sq[i] = rh * rh;
                     }
                     // a chirp whose chirp-level weight (skip test, and the window unless it is
                     // per sample) is zero for every pixel of the warp contributes nothing
@@ -323,16 +331,18 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                         float4 av = make_float4(0.f, 0.f, 0.f, 0.f), bv = av;
                         if (TRAJ) av = as[s];
                         if (WIN) bv = bs[s];
+                        const float uD = TW ? us[s] : 0.0f;
                         const float res = WIDE ? sgr[s] : 0.0f;
                         const float gsv = TRAJ ? sgg[s] : 0.0f;
 #pragma unroll
                         for (int i = 0; i < kPT; ++i) {
                             float yr = xr, yi = xi;
+                            float n = 0.0f;  // N = 2 (P0 - T).D + |D|^2 = |P0 - T + D|^2 - R0^2
                             if (TRAJ || WIDE) {
                                 float psi = 0.0f;
                                 if (TRAJ) {
-                                    // N = 2 (P0 - T).D + |D|^2 (|D|^2 from the table)
-                                    const float n = fmaf(t2x[i], av.x, fmaf(t2y[i], av.y, fmaf(t2z[i], av.z, av.w)));
+                                    // |D|^2 from the table
+                                    n = fmaf(t2x[i], av.x, fmaf(t2y[i], av.y, fmaf(t2z[i], av.z, av.w)));
                                     const float e = n * b2[i];
                                     float f;
                                     if (WIDE) {
@@ -360,13 +370,12 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
                                 // q = (fDop - centre) / B from the table's velocity scaled by
                                 // -2/(lambda B) and centre / B; in band for |q| <= 1/2, taper
                                 // a - (1-a) cos(2 pi q - pi) = a + (1-a) cos(2 pi q)
+                                // (with moving positions: u.d = (u/2).2(P0 - T) + u.D, the second
+                                // term from the table, and |d|^2 = R0^2 + N)
                                 float q;
                                 if (TRAJ) {
-                                    const float dx = fmaf(0.5f, t2x[i], av.x);
-                                    const float dy = fmaf(0.5f, t2y[i], av.y);
-                                    const float dz = fmaf(0.5f, t2z[i], av.z);
-                                    const float rsi = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                                    q = fmaf(fmaf(bv.x, dx, fmaf(bv.y, dy, bv.z * dz)), rsi, -bv.w);
+                                    const float ud = fmaf(bv.x, t2x[i], fmaf(bv.y, t2y[i], fmaf(bv.z, t2z[i], uD)));
+                                    q = fmaf(ud, rsqrtf(r0sq[i] + n), -bv.w);
                                 } else {
                                     q = fmaf(bv.x, t2x[i], fmaf(bv.y, t2y[i], fmaf(bv.z, t2z[i], -bv.w)));
                                 }

@@ -80,7 +80,10 @@ struct FocusJob {
     const double *gs;        // [S] 2 f_s / c0 (FP64 kernels only)
     const float4 *traj;      // [C][s_pad] (P[c,s] - P[c,0], |P[c,s] - P[c,0]|^2) (FP32 general kernel, per-sample positions)
     const float4 *wins;      // [C][s_pad] (velocity x -2/(lambda B), window centre / B) per sample (FP32 general
-                             // kernel, per-sample windows)
+                             // kernel, per-sample windows); the velocity term halved when positions also
+                             // move within chirps
+    const float *wdot;       // [C][s_pad] velocity x -2/(lambda B) . (P[c,s] - P[c,0]) (per-sample positions
+                             // and windows)
     const float *gres;       // [s_pad] 2 f_s / c0 - (g0 + g1 s) (FP32 general kernel, non-uniform sampling)
     const float *gsam;       // [s_pad] 2 f_s / c0 [cycles / m] (wide variants) or 2 pi x that [rad / m]
                              // (narrow variants) (FP32 general kernel, per-sample positions)

@@ -161,7 +161,7 @@ struct tdc_processor {
     tdc::impl::DevBuf xw, chirps, skip, gs, pos_base, wr, offsets, flag;
     // FP32 general path: sample-0 records per chirp (when chirps holds one per sample),
     // per-sample offsets / windows, residual frequency table.
-    tdc::impl::DevBuf gen_rec, traj, wins, gres;
+    tdc::impl::DevBuf gen_rec, traj, wins, wdot, gres;
 
     // Device grid.
     long long P = 0;
@@ -193,7 +193,7 @@ struct tdc_processor {
     std::vector<tdc::impl::DevBuf *> device_buffers()
     {
         return {&xw,      &chirps,     &skip,    &gs,      &pos_base, &wr,      &offsets,     &flag,     &gen_rec,
-                &traj,    &wins,       &gres,    &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch,
+                &traj,    &wins,       &wdot,    &gres,    &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch,
                 &image_dev};
     }
 };
