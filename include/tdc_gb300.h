@@ -138,7 +138,9 @@ typedef struct tdc_start_stats {
     int stage_chirps;     /* chirp rows per pipeline stage (1 when rows are staged in segments) */
     int general_variant;  /* FP32 general kernel variant bits (1 per-sample positions, 2 per-sample
                              windows, 4 wide phase correction); 0 on the other paths */
-    int reserved;
+    int tile_cols;        /* 0: work tiles of 512 consecutive pixels; else tiles of 512 / tile_cols grid
+                             rows x tile_cols columns (finite Doppler band, antenna moving along the
+                             grid's columns) */
 } tdc_start_stats;
 
 typedef enum tdc_path {

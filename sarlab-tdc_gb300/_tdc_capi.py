@@ -121,7 +121,7 @@ class StartStats(C.Structure):
         ("stage_samples", C.c_int),
         ("stage_chirps", C.c_int),
         ("general_variant", C.c_int),
-        ("reserved", C.c_int),
+        ("tile_cols", C.c_int),
     ]
 
     def as_dict(self) -> dict:

@@ -311,6 +311,16 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         for (int c = cb; c < ce; ++c) recs[c] = make_record(p, c, 0, o.centroid != 0, o.center);
     });
     p->sample_recs_ready = false;
+    {
+        double v[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < C; ++c) {
+            v[0] += recs[c].vel.x;
+            v[1] += recs[c].vel.y;
+            v[2] += recs[c].vel.z;
+        }
+        const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int k = 0; k < 3; ++k) p->vel_dir[k] = n > 0.0 ? v[k] / n : 0.0;
+    }
 
     // ---- FP32 general path tables (per-sample trajectories / windows, non-uniform sampling) ----
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
@@ -506,6 +516,13 @@ int upload_grid(tdc_processor *p, int &launches)
     const size_t elt = p->grid64 ? 8 : 4;
     TDC_CK(p->grid_hi.ensure((size_t)P * 16), "alloc grid");
     const void *src = p->grid64 ? (const void *)p->grid64 : (const void *)p->grid;
+    {
+        auto g = [&](long long i, int k) { return p->grid64 ? p->grid64[3 * i + k] : (double)p->grid[3 * i + k]; };
+        for (int k = 0; k < 3; ++k) {
+            p->axis_c[k] = p->cols > 1 ? g(1, k) - g(0, k) : 0.0;
+            p->axis_r[k] = p->rows > 1 ? g(p->cols, k) - g(0, k) : 0.0;
+        }
+    }
     if (!p->host_reads) {
         for (int k = 0; k < 3; ++k) {
             p->grid_min[k] = std::numeric_limits<double>::infinity();
@@ -610,11 +627,35 @@ int choose_path(const tdc_processor *p)
     return TDC_PATH_GENERAL;
 }
 
+// Block tiles: kFocusTile / kBlockTileCols grid rows x kBlockTileCols columns.
+#ifndef TDC_BLOCK_TILES
+#define TDC_BLOCK_TILES 1
+#endif
+constexpr int kBlockTileCols = 16;
+
+// With a finite Doppler band, chirps whose window (or chunk skip test) is zero for every
+// pixel of a warp skip their work, but a CTA's warps wait for one another at each pipeline
+// stage. The window of a pixel follows its direction from the antenna relative to the
+// antenna's velocity, so warps agree on their in-band chirps when the tile is narrow along
+// the velocity: flat tiles (512 consecutive pixels, at most a few grid rows) are narrow
+// across the columns, block tiles (32 rows x 16 columns) along them. Block tiles are used
+// when the band is finite and the velocity runs closer to the grid's column direction than
+// to its row direction; the choice does not change any pixel's value.
+int choose_tile_cols(const tdc_processor *p)
+{
+    if (!TDC_BLOCK_TILES || !std::isfinite(p->opts.bw)) return 0;
+    if (p->cols < 2 * kBlockTileCols || p->rows < kFocusTile / kBlockTileCols) return 0;
+    auto along = [&](const double *a) {
+        const double n = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        return n > 0.0 ? std::fabs(a[0] * p->vel_dir[0] + a[1] * p->vel_dir[1] + a[2] * p->vel_dir[2]) / n : 0.0;
+    };
+    return along(p->axis_c) > along(p->axis_r) ? kBlockTileCols : 0;
+}
+
 // Split the chirps into groups so that tiles x groups units fill whole waves of `slots`;
 // among the splits with at least min_units_per_slot units per slot when there are any.
-void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot)
+void plan_groups(long long n_tiles, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot)
 {
-    const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
     const long long min_units = (long long)min_units_per_slot * slots;
     const int gmax = std::max(1, std::min(C, 1024));
     n_groups = 1;
@@ -820,9 +861,11 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         slots = p->n_sm * 4;
     }
 
+    const int tile_cols = choose_tile_cols(p);
+    const long long n_tiles = tile_count(P, tile_cols, p->cols);
     if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
-        max_unit_work != p->plan_unit_cap) {
-        plan_groups(P, C, slots, p->plan_groups, p->plan_cpg,
+        max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols) {
+        plan_groups(n_tiles, C, slots, p->plan_groups, p->plan_cpg,
                     path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot);
         if (max_unit_work > 0) {
             // bound the work of one unit (tile x chirp group): at most cap / (tile x S) chirps per group
@@ -833,7 +876,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
             }
         }
         p->plan_unit_cap = max_unit_work;
-        const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
+        p->plan_tile_cols = tile_cols;
         p->units_host.clear();
         p->units_host.reserve((size_t)(n_tiles * p->plan_groups));
         for (long long t = 0; t < n_tiles; ++t)
@@ -861,6 +904,9 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     plan.off_units = L.off_units;
     plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
     plan.job.seg_len = path == TDC_PATH_GENERAL ? gen_seg : seg ? kSegmentSamples : 0;
+    plan.job.tile_cols = tile_cols;
+    plan.job.grid_cols = p->cols;
+    plan.job.n_tiles = (int)n_tiles;
     // narrow variants take the phase correction in radians
     if (path == TDC_PATH_GENERAL && !(variant & 4)) plan.job.gsam = p->gres.as<const float>() + 2 * (size_t)p->s_pad;
     return TDC_OK;
@@ -925,13 +971,15 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     int *status = counter + 1;
     if (path == TDC_PATH_FP32_BULK) {
         const int grid = std::min(n_units, slots);
+        // the zero-window-skipping instances also map block tiles (which come with a finite band)
+        const bool skip_zero = std::isfinite(job.half_bw) || job.tile_cols != 0;
         if (plan.seg)
             TDC_CK(launch_focus_fp32_seg(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
-                                         std::isfinite(job.half_bw), st),
+                                         skip_zero, st),
                    "focus kernel (segmented rows)");
         else
-            TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
-                                     std::isfinite(job.half_bw), st),
+            TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, skip_zero,
+                                     st),
                    "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);
@@ -950,6 +998,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     p->stats.stage_samples = staged ? std::min(row, p->s_pad) : 0;
     p->stats.stage_chirps = staged ? (row < p->s_pad ? 1 : plan.cb) : 0;
     p->stats.general_variant = path == TDC_PATH_GENERAL ? plan.variant : 0;
+    p->stats.tile_cols = job.tile_cols;
     return TDC_OK;
 }
 
@@ -1325,7 +1374,7 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     if (bps <= 0) return fail(TDC_ERR_CUDA, "adjoint kernel does not fit on the device");
     const int slots = p->n_sm * bps;
     int n_groups = 1, cpg = C;
-    plan_groups(P, C, slots, n_groups, cpg, kFocusMinUnitsPerSlot);
+    plan_groups((P + kFocusTile - 1) / kFocusTile, C, slots, n_groups, cpg, kFocusMinUnitsPerSlot);
     const long long n_tiles = (P + kFocusTile - 1) / kFocusTile;
     std::vector<FocusUnit> units;
     units.reserve((size_t)(n_tiles * n_groups));

@@ -13,6 +13,22 @@ namespace tdc {
 constexpr float kTwoPiF = 6.28318530717958647692f;
 constexpr float kPiF = 3.14159265358979323846f;
 
+// Pixel of slot `slot` (0 .. kFocusTile-1) of tile `t`, or -1 where the slot lies outside
+// the grid (see FocusJob::tile_cols).
+__device__ __forceinline__ long long tile_pixel(int tile_cols, int grid_cols, long long P, int t, int slot)
+{
+    if (tile_cols <= 0) {
+        const long long p = (long long)t * kFocusTile + slot;
+        return p < P ? p : -1;
+    }
+    const int n_tc = (grid_cols + tile_cols - 1) / tile_cols;
+    const int tr = t / n_tc;
+    const int col = (t - tr * n_tc) * tile_cols + slot % tile_cols;
+    const long long row = (long long)tr * (kFocusTile / tile_cols) + slot / tile_cols;
+    const long long p = row * grid_cols + col;
+    return col < grid_cols && p < P ? p : -1;
+}
+
 // ---------------------------------------------------------------------------
 // Error-free transformations (Knuth two-sum, FMA two-product).
 

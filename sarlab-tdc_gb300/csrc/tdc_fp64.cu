@@ -37,7 +37,6 @@ __global__ void __launch_bounds__(kThreads) focus_fp64_kernel(const FocusJob *__
     const FocusJob &J = jobs[un.job];
     const int tid = threadIdx.x;
     const long long P = J.P;
-    const long long tile_base = (long long)un.tile * kFocusTile;
     const int c0 = un.group * J.chirps_per_group;
     const int c1 = min(J.C, c0 + J.chirps_per_group);
     const int S = J.S, s_pad = J.s_pad;
@@ -51,9 +50,9 @@ __global__ void __launch_bounds__(kThreads) focus_fp64_kernel(const FocusJob *__
     float txh[kPT], tyh[kPT], tzh[kPT];
 #pragma unroll
     for (int i = 0; i < kPT; ++i) {
-        const long long p = tile_base + i * kThreads + tid;
+        const long long p = tile_pixel(J.tile_cols, J.grid_cols, P, un.tile, i * kThreads + tid);
         float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
-        if (p < P) {
+        if (p >= 0) {
             hi = __ldg(&J.grid_hi[p]);
             if (J.grid_lo) lo = __ldg(&J.grid_lo[p]);
         }
@@ -173,8 +172,8 @@ __global__ void __launch_bounds__(kThreads) focus_fp64_kernel(const FocusJob *__
     float4 *__restrict__ part = J.partial + (size_t)un.group * P;
 #pragma unroll
     for (int i = 0; i < kPT; ++i) {
-        const long long pidx = tile_base + i * kThreads + tid;
-        if (pidx < P) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
+        const long long pidx = tile_pixel(J.tile_cols, J.grid_cols, P, un.tile, i * kThreads + tid);
+        if (pidx >= 0) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
     }
 }
 

@@ -184,13 +184,12 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
             for (int j = 0; j < npro; ++j) issue(j);
         }
 
-        const long long tile_base = (long long)un.tile * kTile;
         const long long P = sJ.P;
 #pragma unroll
         for (int i = 0; i < kPT; ++i) {
-            const long long p = tile_base + i * kT + tid;
+            const long long p = tile_pixel(sJ.tile_cols, sJ.grid_cols, P, un.tile, i * kT + tid);
             float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
-            if (p < P) {
+            if (p >= 0) {
                 hi = __ldg(&sJ.grid_hi[p]);
                 if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[p]);
             }
@@ -434,8 +433,8 @@ __global__ void __launch_bounds__(kT, (!TRAJ && WIN && WIDE) ? 1 : TDC_GENERAL_M
         float4 *__restrict__ part = sJ.partial + (size_t)un.group * P;
 #pragma unroll
         for (int i = 0; i < kPT; ++i) {
-            const long long pidx = tile_base + i * kT + tid;
-            if (pidx < P) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
+            const long long pidx = tile_pixel(sJ.tile_cols, sJ.grid_cols, P, un.tile, i * kT + tid);
+            if (pidx >= 0) part[pidx] = make_float4(sum[i].x, sum[i].y, comp[i].x, comp[i].y);
         }
         __syncthreads();
     }

@@ -108,12 +108,24 @@ struct FocusJob {
     float g1_lo;             // low part of g1 (double-float pair)
     int seg_len;             // samples per pipeline stage of a chirp staged in segments (FP32 bulk: 0 for
                              // whole rows; FP32 general: s_pad for whole rows)
+    int tile_cols;           // 0: a tile is kFocusTile consecutive pixels; else kFocusTile / tile_cols grid
+                             // rows x tile_cols columns of the grid_cols-wide row-major grid
+    int grid_cols;           // columns of the focus grid (block tiles)
     int pad_;
 };
 
 // Kernels copy a FocusJob into shared memory one int per thread (128 threads); the
 // no-allocation scratch reserves 256 bytes for it.
 static_assert(sizeof(FocusJob) <= 256 && sizeof(FocusJob) % 8 == 0, "FocusJob layout");
+
+// Tiles of a P-pixel grid (see FocusJob::tile_cols).
+inline long long tile_count(long long P, int tile_cols, int grid_cols)
+{
+    if (tile_cols <= 0 || grid_cols <= 0) return (P + kFocusTile - 1) / kFocusTile;
+    const long long rows = (P + grid_cols - 1) / grid_cols;
+    const int tile_rows = kFocusTile / tile_cols;
+    return ((rows + tile_rows - 1) / tile_rows) * ((grid_cols + tile_cols - 1) / tile_cols);
+}
 
 struct FocusUnit {
     int job;

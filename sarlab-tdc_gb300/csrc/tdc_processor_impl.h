@@ -167,13 +167,15 @@ struct tdc_processor {
     long long P = 0;
     bool grid_lo_valid = false;
     double grid_min[3] = {0, 0, 0}, grid_max[3] = {0, 0, 0};
+    double axis_c[3] = {0, 0, 0}, axis_r[3] = {0, 0, 0};  // grid column / row steps (first pixel's)
+    double vel_dir[3] = {0, 0, 0};                         // mean antenna velocity direction (0: at rest)
     tdc::impl::DevBuf grid_stage, grid_hi, grid_lo;
 
     // Focus plan cache + scratch.
     tdc::impl::DevBuf scratch;
     std::vector<tdc::FocusUnit> units_host;
     long long plan_P = -1;
-    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0;
+    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0, plan_tile_cols = -1;
     double plan_unit_cap = 0.0;
     bool plan_uploaded = false;
 
@@ -217,7 +219,9 @@ struct FocusPlan {
 int prepare(tdc_processor *p, const StartOpts &o, int &launches);
 int upload_grid(tdc_processor *p, int &launches);
 int choose_path(const tdc_processor *p);
-void plan_groups(long long P, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot);
+void plan_groups(long long n_tiles, int C, int slots, int &n_groups, int &cpg, int min_units_per_slot);
+// Tile shape of the resident grid: 0 (flat tiles) or the columns of a block tile.
+int choose_tile_cols(const tdc_processor *p);
 int stage_bytes_for(int s_pad, int &cb);
 // True when a whole row of s_pad samples does not fit the FP32-bulk kernel's stages.
 bool needs_segments(int s_pad);

@@ -100,7 +100,8 @@ size_t device_footprint(const tdc_job_desc &d, int n_sm)
     const size_t C = (size_t)d.n_pri, S = (size_t)d.n_samples, P = (size_t)d.n_pix;
     const size_t s_pad = round_up(S, kSampleAlign);
     int groups = 1, cpg = d.n_pri;
-    plan_groups((long long)P, d.n_pri, std::max(1, n_sm * 3), groups, cpg, kFocusMinUnitsPerSlot);
+    plan_groups(((long long)P + kFocusTile - 1) / kFocusTile, d.n_pri, std::max(1, n_sm * 3), groups, cpg,
+                kFocusMinUnitsPerSlot);
     const int cpg_cap = std::max(1, (int)(kServerUnitWork / ((double)kFocusTile * S)));
     if (cpg > cpg_cap) groups = (d.n_pri + cpg_cap - 1) / cpg_cap;
     const size_t n_tiles = (P + kFocusTile - 1) / kFocusTile;

@@ -8,6 +8,8 @@ synthetic shapes with the acquisition and grid resident on the device:
     2: 1024^2 pixels x 4096 chirps x 1024 samples (the precision-study size)
     3: 1024^2 pixels x 4096 chirps x  256 samples (the 3-D volume's sample count)
     1: 256^2 pixels x 1024 chirps x 512 samples (the small stripmap case)
+    2b: shape 2 with the antenna moving at 0.05 m/s along the rail and a 10 Hz Doppler
+        band (windowed focus: zero-window chirps skipped)
 
 and, for the general kernel (TDC_GENERAL_PT, TDC_GENERAL_MINB, TDC_GENERAL_STAGE_TARGET,
 TDC_GENERAL_ALWAYS_SEGMENT),
@@ -56,9 +58,14 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
     elif shape.startswith("g"):
         sc = scenes.config2(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
     else:
-        sc = scenes.config2(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=1024 if shape == "2" else 256,
+        sc = scenes.config2(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=256 if shape == "3" else 1024,
                             n_targets=8)
     api = sc.api_arrays()
+    if shape == "2b":
+        vel = np.zeros((sc.n_pri, sc.n_samples, 3), np.float32)
+        vel[..., 0] = 0.05
+        api["velocity"] = vel
+        band = 10.0
     p = _sarlabtdc.TdcProcessor(0)
     if shape.startswith("g"):
         C, S = sc.n_pri, sc.n_samples

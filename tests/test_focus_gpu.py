@@ -550,3 +550,27 @@ def test_parity_ragged_shapes(cuda_device, n_pri, n_samples, nx, ny):
             _check(img, ref, l2=2e-4, phase=None)
         else:
             _check(img, ref)
+
+
+@pytest.mark.parametrize("general", [False, True])
+def test_block_tiles_under_a_finite_band(cuda_device, general):
+    """A finite Doppler band with the antenna moving along the grid's columns: the work
+    tiles become blocks of 32 rows x 16 columns (ragged at the grid's edges: 40 x 35
+    pixels); parity with the oracle on the bulk and the general kernel, and flat tiles
+    again for an unbounded band."""
+    sc = scenes.small_scene(seed=93, n_pri=400, n_samples=48, nx=40, ny=35, rail_len=0.4, device="cuda")
+    api = _moving_api(sc, speed=0.08)
+    if general:
+        api = _general_api(sc, traj=True)
+        api["velocity"] = _moving_api(sc, speed=0.08)["velocity"]
+    args = (0.0, 14.0, False, True, True)
+    img, stats, _ = run_engine(api, sc.grid, args)
+    assert stats["path_name"] == ("general" if general else "fp32_bulk")
+    assert stats["tile_cols"] == 16
+    ref = _oracle(api, sc.grid, args).reshape(img.shape)
+    full = _oracle(api, sc.grid, (0.0, INF, False, True, True)).reshape(img.shape)
+    assert rel_l2(ref, full) > 0.05  # the band must zero part of the image
+    _check(img, ref, l2=2e-4, phase=None)
+    img_inf, stats_inf, _ = run_engine(api, sc.grid, (0.0, INF, False, True, True))
+    assert stats_inf["tile_cols"] == 0
+    _check(img_inf, full)
