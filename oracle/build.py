@@ -5,7 +5,7 @@
 * ``oracle/_ref/tdckernels.ptx`` -- the reference's own GPU kernels
   (``tdc-lib/src/tdckernels.cu``) compiled to PTX by nvcc from where the source
   lies in the reference checkout (fmt from torch's bundled headers). PTX is
-  architecture-neutral text, so it travels to the GPU machine, where
+  architecture-neutral text, so it can be loaded on any machine with a GB300, where
   tests/golden/make_ref_gpu_golden.py runs those kernels to record golden images.
 * ``oracle/_ref/libtdc_refmath.so`` -- the reference's own host-side math
   (``tdc-lib/include/gpumath.h`` and ``windowing.h``, compiled from where they
