@@ -41,7 +41,7 @@ typedef enum tdc_status {
     TDC_ERR_STATE = -3,            /* call order violated (start before setRawData / setFocusGrid) */
     TDC_ERR_NO_MEMORY = -4,        /* device or pinned host allocation failed */
     TDC_ERR_TIMEOUT = -5,          /* a kernel's bounded wait expired; the kernel returned early */
-    TDC_ERR_UNSUPPORTED = -6,      /* input outside what this build handles (message says which) */
+    TDC_ERR_UNSUPPORTED = -6,      /* input outside what this library handles (message says which) */
     TDC_ERR_SHAPE = -7             /* array shape mismatch (runtime_error in the pybind wrapper) */
 } tdc_status;
 

@@ -1,7 +1,7 @@
 /*
  * tdc_oracle.c -- FP64 CPU restatement of the sarlab-tdc focus path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker: it is built and called by
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle: it is built and called by
  * tests/, by __graft_entry__.smoke() and by bench.py's cpu_baseline / reference
  * arm, and never by the product library (sarlab-tdc_gb300/), which has no CPU
  * fallback.
