@@ -153,11 +153,11 @@ def make_scene(args, device):
 
     t = time.time()
     if args.config == "1":
-        sc = scenes.config1(device=device)
+        sc = scenes.stripmap(device=device)
     elif args.config == "3":
-        sc = scenes.config3(device=device)
+        sc = scenes.volume_3d(device=device)
     else:
-        sc = scenes.config2(device=device, n_pix_side=args.side, n_pri=args.chirps, n_samples=args.samples)
+        sc = scenes.precision_study(device=device, n_pix_side=args.side, n_pri=args.chirps, n_samples=args.samples)
     log(f"scene: {sc.n_pix} px x {sc.n_pri} chirps x {sc.n_samples} samples "
         f"({sc.correlations() / 1e9:.1f} Gcorr) generated in {time.time() - t:.1f}s")
     return sc
@@ -651,7 +651,7 @@ def run_autofocus(args):
     import oracle
     from sarlabtdc import autofocus, scenes
 
-    sc = scenes.config5(device="cuda")
+    sc = scenes.autofocus_scene(device="cuda")
     api = sc.api_arrays()
     p = _sarlabtdc.TdcProcessor(0)
     p.setRawData(*api.values())

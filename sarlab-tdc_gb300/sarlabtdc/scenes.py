@@ -141,7 +141,7 @@ def rail(n: int, length: float, height: float) -> np.ndarray:
     return pos
 
 
-def config1(seed=1, device="cpu", n_pix_side=256, n_pri=1024, n_samples=512, simulate=True) -> Scene:
+def stripmap(seed=1, device="cpu", n_pix_side=256, n_pri=1024, n_samples=512, simulate=True) -> Scene:
     """Plain TDC stripmap: 512 samples, 1024 chirps on a 0.5 m rail (0.5 mm), 0.3 m above
     a 256 x 256 ground grid at 2 mm; 3 unit targets; 20 dB SNR; Hann."""
     rng = np.random.default_rng(seed)
@@ -152,13 +152,13 @@ def config1(seed=1, device="cpu", n_pix_side=256, n_pri=1024, n_samples=512, sim
     tg = np.zeros((3, 3))
     tg[:, 0] = rng.uniform(lo[0], hi[0], 3)
     tg[:, 1] = rng.uniform(lo[1], hi[1], 3)
-    sc = Scene("config1", radar, pos, grid, tg, np.ones(3, np.complex128))
+    sc = Scene("stripmap", radar, pos, grid, tg, np.ones(3, np.complex128))
     if simulate:
         finish_raw(sc, simulate_raw(pos, tg, sc.amps, radar, device), 20.0, rng)
     return sc
 
 
-def config2(seed=2, device="cpu", n_pix_side=1024, n_pri=4096, n_samples=1024, n_targets=50,
+def precision_study(seed=2, device="cpu", n_pix_side=1024, n_pri=4096, n_samples=1024, n_targets=50,
             simulate=True) -> Scene:
     """Precision study: 1024 samples, 4096 chirps over 2 m with 0.5 mm/axis jitter (FP64
     positions), 1024 x 1024 grid at 1 mm, 50 Rayleigh targets."""
@@ -171,13 +171,13 @@ def config2(seed=2, device="cpu", n_pix_side=1024, n_pri=4096, n_samples=1024, n
     tg[:, 0] = rng.uniform(lo[0], hi[0], n_targets)
     tg[:, 1] = rng.uniform(lo[1], hi[1], n_targets)
     amps = rng.rayleigh(1.0, n_targets) * np.exp(2j * np.pi * rng.uniform(0, 1, n_targets))
-    sc = Scene("config2", radar, pos, grid, tg, amps)
+    sc = Scene("precision_study", radar, pos, grid, tg, amps)
     if simulate:
         finish_raw(sc, simulate_raw(pos, tg, amps, radar, device), 20.0, rng)
     return sc
 
 
-def config3(seed=3, device="cpu", nx=256, nz=256, ny=64, n_ap=128, n_samples=256, n_targets=200,
+def volume_3d(seed=3, device="cpu", nx=256, nz=256, ny=64, n_ap=128, n_samples=256, n_targets=200,
             simulate=True) -> Scene:
     """3-D near field: 128 x 128 planar aperture at 1 mm (x-z plane, y = 0), 256 samples,
     256 x 256 x 64 voxels (1 mm lateral, 2 mm depth from 0.2 m), 200 scatterers, 15 dB."""
@@ -199,13 +199,13 @@ def config3(seed=3, device="cpu", nx=256, nz=256, ny=64, n_ap=128, n_samples=256
     tg = np.stack([rng.uniform(xs[0], xs[-1], n_targets), rng.uniform(ys[0], ys[-1], n_targets),
                    rng.uniform(zs[0], zs[-1], n_targets)], axis=1)
     amps = np.exp(2j * np.pi * rng.uniform(0, 1, n_targets))
-    sc = Scene("config3", radar, pos, grid, tg, amps)
+    sc = Scene("volume_3d", radar, pos, grid, tg, amps)
     if simulate:
         finish_raw(sc, simulate_raw(pos, tg, amps, radar, device), 15.0, rng)
     return sc
 
 
-def config5(seed=5, device="cpu", n_pix_side=512, n_pri=4096, n_samples=1024, n_targets=30,
+def autofocus_scene(seed=5, device="cpu", n_pix_side=512, n_pri=4096, n_samples=1024, n_targets=30,
             step_sigma=0.2e-3, simulate=True) -> Scene:
     """Autofocus: 4096 chirps x 1024 samples over 2 m, true trajectory = nominal rail + a
     random walk (0.2 mm per step per axis); 512 x 512 grid at 1 mm; 30 targets.
@@ -222,7 +222,7 @@ def config5(seed=5, device="cpu", n_pix_side=512, n_pri=4096, n_samples=1024, n_
     tg[:, 0] = rng.uniform(lo[0], hi[0], n_targets)
     tg[:, 1] = rng.uniform(lo[1], hi[1], n_targets)
     amps = rng.rayleigh(1.0, n_targets) * np.exp(2j * np.pi * rng.uniform(0, 1, n_targets))
-    sc = Scene("config5", radar, nominal, grid, tg, amps, meta={"walk": walk, "true_positions": true_pos})
+    sc = Scene("autofocus_scene", radar, nominal, grid, tg, amps, meta={"walk": walk, "true_positions": true_pos})
     if simulate:
         finish_raw(sc, simulate_raw(true_pos, tg, amps, radar, device), 20.0, rng)
     return sc
@@ -230,7 +230,7 @@ def config5(seed=5, device="cpu", n_pix_side=512, n_pri=4096, n_samples=1024, n_
 
 def small_scene(seed=0, n_pri=256, n_samples=128, nx=24, ny=20, n_targets=3, jitter=0.0, snr_db=20.0,
                 device="cpu", rail_len=None, spacing=2e-3, y0=0.12, height=0.3) -> Scene:
-    """A config-1-shaped scene small enough for an FP64 CPU check in a test."""
+    """A stripmap scene (rail above a ground grid) small enough for an FP64 CPU check in a test."""
     rng = np.random.default_rng(seed)
     radar = Radar(n_samples=n_samples)
     pos = rail(n_pri, rail_len if rail_len is not None else n_pri * 0.5e-3, height)

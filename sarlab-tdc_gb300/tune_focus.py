@@ -51,14 +51,14 @@ def _time_shape(shape: str, ref_dir: Path) -> dict:
 
     band = float("inf")
     if shape == "1":
-        sc = scenes.config1(device="cuda")
+        sc = scenes.stripmap(device="cuda")
     elif shape in ("gl", "gs"):
-        sc = scenes.config2(device="cuda", n_pix_side=256, n_pri=256, n_samples=4096 if shape == "gl" else 1024,
+        sc = scenes.precision_study(device="cuda", n_pix_side=256, n_pri=256, n_samples=4096 if shape == "gl" else 1024,
                             n_targets=8)
     elif shape.startswith("g"):
-        sc = scenes.config2(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
+        sc = scenes.precision_study(device="cuda", n_pix_side=512, n_pri=1024, n_samples=1024, n_targets=8)
     else:
-        sc = scenes.config2(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=256 if shape == "3" else 1024,
+        sc = scenes.precision_study(device="cuda", n_pix_side=1024, n_pri=4096, n_samples=256 if shape == "3" else 1024,
                             n_targets=8)
     api = sc.api_arrays()
     if shape == "2b":

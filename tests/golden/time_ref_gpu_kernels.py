@@ -44,7 +44,7 @@ def main() -> int:
         print(json.dumps({"error": "oracle/_ref/tdckernels.ptx is missing"}))
         return 1
     drv = ref.Driver(Path(ptx).read_bytes())
-    sc = {"1": scenes.config1, "2": scenes.config2, "3": scenes.config3}[workload](device="cuda")
+    sc = {"1": scenes.stripmap, "2": scenes.precision_study, "3": scenes.volume_3d}[workload](device="cuda")
     C_, S = sc.n_pri, sc.n_samples
     rng = np.random.default_rng(7)
     flat = sc.grid.reshape(-1, 3)
