@@ -141,6 +141,8 @@ typedef struct tdc_start_stats {
     int tile_cols;        /* 0: work tiles of 512 consecutive pixels; else tiles of 512 / tile_cols grid
                              rows x tile_cols columns (finite Doppler band, antenna moving along the
                              grid's columns) */
+    int adjoint_stored;   /* the last adjoint read the kept per-chirp sums (1) or recomputed them (0) */
+    int reserved;
 } tdc_start_stats;
 
 typedef enum tdc_path {
@@ -233,9 +235,20 @@ int tdc_processor_set_chirp_offsets_device(tdc_processor *proc, const double *of
  * (n_pix complex floats, dL/dRe I + j dL/dIm I, as torch stores the gradient
  * of a complex tensor). The Doppler window and skip test are held fixed. The
  * reference response is recomputed, not stored. Blocking. FP32-bulk path only.
+ * After a focus that kept its per-chirp sums (tdc_processor_set_keep_chirp_sums)
+ * on the same acquisition, trajectory and grid, ordered before this call on the
+ * device, the adjoint reads them and recomputes only the index-weighted sums
+ * (half the arithmetic); otherwise it recomputes both.
  */
 int tdc_processor_adjoint_device(tdc_processor *proc, const float *grad_image_dev, double *grad_offsets_dev,
                                  void *stream);
+
+/* keep != 0: device-resident focuses on the FP32-bulk path (whole rows) also write their
+ * per-(chirp, pixel) sums A = sum_s x_s z^s, n_pri x n_pix complex floats, for the next
+ * adjoint, when they fit in half the free device memory; keep = 0 frees them. Changing
+ * the trajectory (tdc_processor_set_chirp_offsets_device), the grid or the prepared
+ * acquisition makes kept sums stale: the adjoint then recomputes. */
+int tdc_processor_set_keep_chirp_sums(tdc_processor *proc, int keep);
 
 /* ---- request loop (no reference counterpart) ---- */
 

@@ -285,6 +285,11 @@ class TdcProcessor:
         go = _device_buffer(grad_offsets, "float64", 3 * self.numChirps(), "grad_offsets")
         _lib.check(_lib.lib().tdc_processor_adjoint_device(self._h, gi, go, self._stream(stream)))
 
+    def keepChirpSums(self, keep=True):
+        """Let device-resident focuses keep their per-chirp sums for the next adjointDevice
+        (which then does half the arithmetic); False frees them."""
+        _lib.check(_lib.lib().tdc_processor_set_keep_chirp_sums(self._h, int(bool(keep))))
+
     def check(self, stream=None):
         """Synchronise ``stream`` and raise if a focus kernel reported an error."""
         _lib.check(_lib.lib().tdc_processor_check(self._h, self._stream(stream)))

@@ -122,6 +122,8 @@ class StartStats(C.Structure):
         ("stage_chirps", C.c_int),
         ("general_variant", C.c_int),
         ("tile_cols", C.c_int),
+        ("adjoint_stored", C.c_int),
+        ("reserved", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -167,6 +169,7 @@ SIGNATURES = [
     ("tdc_focus_noalloc_async", C.c_int, [C.POINTER(NoallocFocusArgs), _vp, _vp, _vp]),
     ("tdc_processor_set_chirp_offsets_device", C.c_int, [_vp, _vp, _vp]),
     ("tdc_processor_adjoint_device", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("tdc_processor_set_keep_chirp_sums", C.c_int, [_vp, C.c_int]),
     ("tdc_server_create", C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(_vp)]),
     ("tdc_server_submit", C.c_int, [_vp, C.POINTER(JobDesc), C.POINTER(C.c_uint64)]),
     ("tdc_server_wait", C.c_int, [_vp, C.c_uint64, C.c_int, C.POINTER(JobInfo)]),

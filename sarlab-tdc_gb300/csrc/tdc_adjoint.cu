@@ -13,10 +13,14 @@
 // Horner scheme: over blocks b (last first), with y_b = sum_k x_{bL+k} p_k and
 // y'_b = sum_k k x_{bL+k} p_k,
 //   A <- A QL + y_b,     B <- (B + L A_old) QL + y'_b,
-// i.e. 8 FFMA per correlation. The reference response is recomputed per tile
-// and never stored. Per chirp the CTA reduces its pixels' contributions
-// (warp shuffles + shared memory) into one float4 per (tile, chirp); an FP64
-// kernel sums the tiles in order, so the gradient is deterministic.
+// i.e. 8 FFMA per correlation. With the forward's sums A stored per (chirp, pixel)
+// (the storing focus instance) and the rows staged pre-scaled by the sample index,
+// x'_s = s x_s, B is the forward's own recurrence over x' (B <- B QL + sum_k x'_k p_k,
+// 8-entry table): 4 FFMA per correlation, and A is read back. Either way the
+// reference response is recomputed per tile and never stored. Per chirp the CTA
+// reduces its pixels' contributions (warp shuffles + shared memory) into one float4
+// per (tile, chirp); an FP64 kernel sums the tiles in order, so the gradient is
+// deterministic.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,7 +31,8 @@ namespace tdc {
 
 namespace {
 
-constexpr int kLA = 4;  // in-block table length of the adjoint (two tables per pixel)
+constexpr int kLA = 4;  // in-block table length of the coupled recurrence (two tables per pixel)
+constexpr int kLS = 8;  // in-block table length with stored sums (one table, as in the forward)
 
 struct AdjShared {
     float t[kFocusPT * 6][kFocusThreads];  // pixel coordinates (hi xyz, lo xyz)
@@ -39,6 +44,7 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
+template <bool STORED>
 __global__ void __launch_bounds__(kFocusThreads, 3)
     adjoint_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                         int *__restrict__ counter, int *__restrict__ status, int stage_bytes,
@@ -125,7 +131,9 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
         const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
         const int chunk = sJ.chunk;
         const SkipPoint *__restrict__ skip = sJ.skip;
-        const int nb = s_pad / kLA;
+        constexpr int kL = STORED ? kLS : kLA;
+        const int nb = s_pad / kL;
+        const float2 *__restrict__ sums = sJ.chirp_sums;
 
         float wskip[kFocusPT];
 #pragma unroll
@@ -166,7 +174,7 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
                 const ChirpRec r = recs[cc];
                 const float4 *xs = xs_stage + (size_t)cc * (s_pad / 2);
 
-                float2 p[kFocusPT][kLA - 1], kp[kFocusPT][kLA - 1];
+                float2 p[kFocusPT][kL - 1], kp[kFocusPT][STORED ? 1 : kLA - 1];
                 float2 ql[kFocusPT], q0[kFocusPT], A[kFocusPT], B[kFocusPT];
                 float ux[kFocusPT], uy[kFocusPT], uz[kFocusPT];
 #pragma unroll
@@ -187,12 +195,14 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
                     __sincosf(kTwoPiF * (bh + bl), &s1, &c1s);
                     p[i][0] = make_float2(c1s, s1);
 #pragma unroll
-                    for (int k = 1; k < kLA - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
+                    for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
+                    if (!STORED) {
 #pragma unroll
-                    for (int k = 0; k < kLA - 1; ++k)
-                        kp[i][k] = make_float2((float)(k + 1) * p[i][k].x, (float)(k + 1) * p[i][k].y);
-                    const float lbh = (float)kLA * bh;
-                    const float lfr = (lbh - rintf(lbh)) + (float)kLA * bl;
+                        for (int k = 0; k < kLA - 1; ++k)
+                            kp[i][k] = make_float2((float)(k + 1) * p[i][k].x, (float)(k + 1) * p[i][k].y);
+                    }
+                    const float lbh = (float)kL * bh;
+                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
                     float sl, cl;
                     sincospif(2.0f * lfr, &sl, &cl);
                     ql[i] = make_float2(cl, sl);
@@ -209,7 +219,38 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
                     B[i] = make_float2(0.f, 0.f);
                 }
 
-                for (int b = nb - 1; b >= 0; --b) {
+                if (STORED) {
+                    // B = sum_s x'_s z^s over the pre-scaled rows, the forward's recurrence
+                    for (int b = nb - 1; b >= 0; --b) {
+                        float4 xv[kLS / 2];
+#pragma unroll
+                        for (int m = 0; m < kLS / 2; ++m) xv[m] = xs[b * (kLS / 2) + m];
+#pragma unroll
+                        for (int i = 0; i < kFocusPT; ++i) {
+                            float br = fmaf(B[i].x, ql[i].x, xv[0].x);
+                            br = fmaf(-B[i].y, ql[i].y, br);
+                            float bi = fmaf(B[i].x, ql[i].y, xv[0].y);
+                            bi = fmaf(B[i].y, ql[i].x, bi);
+#pragma unroll
+                            for (int k = 1; k < kLS; ++k) {
+                                const float xr = (k & 1) ? xv[k >> 1].z : xv[k >> 1].x;
+                                const float xi = (k & 1) ? xv[k >> 1].w : xv[k >> 1].y;
+                                br = fmaf(xr, p[i][k - 1].x, br);
+                                br = fmaf(-xi, p[i][k - 1].y, br);
+                                bi = fmaf(xr, p[i][k - 1].y, bi);
+                                bi = fmaf(xi, p[i][k - 1].x, bi);
+                            }
+                            B[i] = make_float2(br, bi);
+                        }
+                    }
+                    // A as the forward computed it (zero where its window vote skipped the chirp)
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) {
+                        const long long px = tile_base + i * kFocusThreads + tid;
+                        A[i] = px < P ? sums[(size_t)c * P + px] : make_float2(0.f, 0.f);
+                    }
+                }
+                for (int b = STORED ? -1 : nb - 1; b >= 0; --b) {
                     const float4 xa = xs[b * 2], xb = xs[b * 2 + 1];
                     const float xr[kLA] = {xa.x, xa.z, xb.x, xb.z};
                     const float xi[kLA] = {xa.y, xa.w, xb.y, xb.w};
@@ -227,14 +268,14 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
                         ai = fmaf(A[i].y, ql[i].x, ai);
 #pragma unroll
                         for (int k = 1; k < kLA; ++k) {
-                            ar = fmaf(xr[k], p[i][k - 1].x, ar);
-                            ar = fmaf(-xi[k], p[i][k - 1].y, ar);
-                            ai = fmaf(xr[k], p[i][k - 1].y, ai);
-                            ai = fmaf(xi[k], p[i][k - 1].x, ai);
-                            br = fmaf(xr[k], kp[i][k - 1].x, br);
-                            br = fmaf(-xi[k], kp[i][k - 1].y, br);
-                            bi = fmaf(xr[k], kp[i][k - 1].y, bi);
-                            bi = fmaf(xi[k], kp[i][k - 1].x, bi);
+                            ar = fmaf(xr[k], p[i][STORED ? 0 : k - 1].x, ar);
+                            ar = fmaf(-xi[k], p[i][STORED ? 0 : k - 1].y, ar);
+                            ai = fmaf(xr[k], p[i][STORED ? 0 : k - 1].y, ai);
+                            ai = fmaf(xi[k], p[i][STORED ? 0 : k - 1].x, ai);
+                            br = fmaf(xr[k], kp[i][STORED ? 0 : k - 1].x, br);
+                            br = fmaf(-xi[k], kp[i][STORED ? 0 : k - 1].y, br);
+                            bi = fmaf(xr[k], kp[i][STORED ? 0 : k - 1].y, bi);
+                            bi = fmaf(xi[k], kp[i][STORED ? 0 : k - 1].x, bi);
                         }
                         A[i] = make_float2(ar, ai);
                         B[i] = make_float2(br, bi);
@@ -330,26 +371,26 @@ int adjoint_fp32_smem_bytes(int stage_bytes, int stage_chirps)
     return kFocusStages * stage_bytes + (int)sizeof(AdjShared) + stage_chirps * 4 * 3 * (int)sizeof(float);
 }
 
-int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps)
+int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps, bool stored)
 {
     const int smem = adjoint_fp32_smem_bytes(stage_bytes, stage_chirps);
-    if (allow_max_dynamic_smem(adjoint_fp32_kernel) != cudaSuccess) return 0;
+    auto fn = stored ? adjoint_fp32_kernel<true> : adjoint_fp32_kernel<false>;
+    if (allow_max_dynamic_smem(fn) != cudaSuccess) return 0;
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, adjoint_fp32_kernel, kFocusThreads, smem) !=
-        cudaSuccess)
-        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kFocusThreads, smem) != cudaSuccess) return 0;
     return blocks;
 }
 
 cudaError_t launch_adjoint_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
                                 int *status_dev, int stage_bytes, int stage_chirps, int grid_ctas,
-                                const float2 *gimg, float4 *gpart, cudaStream_t st)
+                                const float2 *gimg, float4 *gpart, bool stored, cudaStream_t st)
 {
     const int smem = adjoint_fp32_smem_bytes(stage_bytes, stage_chirps);
-    cudaError_t e = allow_max_dynamic_smem(adjoint_fp32_kernel);
+    auto fn = stored ? adjoint_fp32_kernel<true> : adjoint_fp32_kernel<false>;
+    cudaError_t e = allow_max_dynamic_smem(fn);
     if (e != cudaSuccess) return e;
-    adjoint_fp32_kernel<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
-                                                                 status_dev, stage_bytes, gimg, gpart);
+    fn<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev, status_dev, stage_bytes,
+                                               gimg, gpart);
     return cudaGetLastError();
 }
 

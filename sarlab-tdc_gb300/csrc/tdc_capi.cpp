@@ -501,6 +501,8 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 
     p->opts = o;
     p->prepared = true;
+    p->xs_scaled_ready = false;
+    ++p->state_epoch;
     p->plan_path = -1;  // job parameters changed
     return TDC_OK;
 }
@@ -512,6 +514,7 @@ int upload_grid(tdc_processor *p, int &launches)
     if (!p->has_grid) return fail(TDC_ERR_STATE, "setFocusGrid must be called before start()");
     const long long P = (long long)p->rows * p->cols;
     p->P = P;
+    ++p->state_epoch;
     cudaStream_t st = p->stream;
     const size_t elt = p->grid64 ? 8 : 4;
     TDC_CK(p->grid_hi.ensure((size_t)P * 16), "alloc grid");
@@ -955,6 +958,19 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     struct {
         size_t off_job, off_units;
     } L{plan.off_job, plan.off_units};
+    // Autofocus: keep the per-(chirp, pixel) sums for the adjoint when they fit in half the
+    // free device memory (whole-row FP32-bulk focus only).
+    bool store = false;
+    if (p->keep_sums && path == TDC_PATH_FP32_BULK && !plan.seg && p->per_chirp) {
+        const size_t bytes = (size_t)C * (size_t)P * sizeof(float2);
+        size_t free_b = 0, total_b = 0;
+        if (bytes <= p->chirp_sums.cap ||
+            (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes + p->chirp_sums.cap <= free_b / 2)) {
+            store = p->chirp_sums.ensure(bytes) == cudaSuccess;
+            if (!store) (void)cudaGetLastError();
+        }
+    }
+    plan.job.chirp_sums = store ? p->chirp_sums.as<float2>() : nullptr;
     const FocusJob &job = plan.job;
 
     TDC_CK(cudaMemcpyAsync(scr + L.off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");
@@ -979,7 +995,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
                    "focus kernel (segmented rows)");
         else
             TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, skip_zero,
-                                     st),
+                                     store, st),
                    "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);
@@ -991,6 +1007,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     }
     TDC_CK(launch_focus_reduce(job.partial, p->plan_groups, P, image_dev, st), "reduce kernel");
     launches += 2;
+    p->sums_epoch = store ? p->state_epoch : 0;
     p->stats.path = path;
     p->stats.correlations = (int64_t)P * C * p->S;
     const bool staged = path == TDC_PATH_FP32_BULK || path == TDC_PATH_GENERAL;
@@ -1340,6 +1357,19 @@ int tdc_processor_path(const tdc_processor *p)
     return choose_path(p);
 }
 
+int tdc_processor_set_keep_chirp_sums(tdc_processor *p, int keep)
+{
+    if (int rc = check_proc(p)) return rc;
+    p->keep_sums = keep != 0;
+    if (!p->keep_sums) {
+        p->chirp_sums.release();
+        p->xs_scaled.release();
+        p->xs_scaled_ready = false;
+        p->sums_epoch = 0;
+    }
+    return TDC_OK;
+}
+
 int tdc_processor_set_chirp_offsets_device(tdc_processor *p, const double *offsets_dev, void *stream)
 {
     if (int rc = check_proc(p)) return rc;
@@ -1349,6 +1379,7 @@ int tdc_processor_set_chirp_offsets_device(tdc_processor *p, const double *offse
     TDC_CK(launch_chirp_positions(p->chirps.as<ChirpRec>(), p->pos_base.as<const double>(), offsets_dev, p->C,
                                   static_cast<cudaStream_t>(stream)),
            "chirp positions kernel");
+    ++p->state_epoch;
     return TDC_OK;
 }
 
@@ -1370,7 +1401,16 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     const int C = p->C;
     int cb = 1;
     const int stage_bytes = stage_bytes_for(p->s_pad, cb);
-    const int bps = adjoint_fp32_blocks_per_sm(stage_bytes, cb);
+    // The forward's sums are usable when a storing focus ran on the current acquisition,
+    // trajectory and grid (stream-ordered before this call).
+    const bool stored = p->keep_sums && p->sums_epoch != 0 && p->sums_epoch == p->state_epoch && p->chirp_sums.p;
+    if (stored && !p->xs_scaled_ready) {
+        TDC_CK(p->xs_scaled.ensure((size_t)C * p->s_pad * sizeof(float2)), "alloc scaled rows");
+        TDC_CK(launch_scale_rows(p->xw.as<const float2>(), C, p->s_pad, p->xs_scaled.as<float2>(), st),
+               "scale rows kernel");
+        p->xs_scaled_ready = true;
+    }
+    const int bps = adjoint_fp32_blocks_per_sm(stage_bytes, cb, stored);
     if (bps <= 0) return fail(TDC_ERR_CUDA, "adjoint kernel does not fit on the device");
     const int slots = p->n_sm * bps;
     int n_groups = 1, cpg = C;
@@ -1389,6 +1429,10 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     FocusJob job = make_job(p, nullptr, cb, TDC_PATH_FP32_BULK);
     job.n_groups = n_groups;
     job.chirps_per_group = cpg;
+    if (stored) {
+        job.xw = p->xs_scaled.as<const float4>();
+        job.chirp_sums = p->chirp_sums.as<float2>();
+    }
     TDC_CK(cudaMemcpyAsync(scr + off_job, &job, sizeof(job), cudaMemcpyHostToDevice, st), "copy job");
     TDC_CK(cudaMemcpyAsync(scr + off_units, units.data(), units.size() * sizeof(FocusUnit), cudaMemcpyHostToDevice,
                            st),
@@ -1399,8 +1443,9 @@ int tdc_processor_adjoint_device(tdc_processor *p, const float *grad_image_dev, 
     TDC_CK(launch_adjoint_fp32(reinterpret_cast<const FocusJob *>(scr + off_job),
                                reinterpret_cast<const FocusUnit *>(scr + off_units), (int)units.size(),
                                reinterpret_cast<int *>(scr), reinterpret_cast<int *>(scr) + 1, stage_bytes, cb, grid,
-                               reinterpret_cast<const float2 *>(grad_image_dev), gpart, st),
+                               reinterpret_cast<const float2 *>(grad_image_dev), gpart, stored, st),
            "adjoint kernel");
+    p->stats.adjoint_stored = stored ? 1 : 0;
     TDC_CK(launch_adjoint_reduce(gpart, (int)n_tiles, C, grad_offsets_dev, st), "adjoint reduce kernel");
     // The host copies above are from stack/vector memory: finish before they go out of scope,
     // and collect the kernel's status word.

@@ -154,7 +154,9 @@ __device__ __forceinline__ bool unit_pixel_ok(long long p, long long P)
 // SKIP_ZERO: chirps whose window is zero for a whole warp skip the Horner loop (launched
 // when a job's Doppler band is finite; with an unbounded band no window is zero, and the
 // plain instance keeps the hot loop's schedule).
-template <bool SKIP_ZERO>
+// STORE: also write each (pixel, chirp) sum A = sum_s x_s z^s (before the start phasor q0) to
+// job.chirp_sums[c][p], zero for chirps skipped by the window vote (the adjoint reads them).
+template <bool SKIP_ZERO, bool STORE>
 __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                       int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
@@ -253,6 +255,16 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
             comp[i] = make_float2(0.f, 0.f);
             wskip[i] = 1.0f;
         }
+        static_assert(kFocusPT == 4, "store_sums takes four pixel slots");
+        auto store_sums = [&](int c, float2 a0, float2 a1, float2 a2, float2 a3) {
+            const float2 a[4] = {a0, a1, a2, a3};
+            float2 *__restrict__ out = sJ.chirp_sums + (size_t)c * P;
+#pragma unroll
+            for (int i = 0; i < kFocusPT; ++i) {
+                const long long px = unit_pixel<SKIP_ZERO>(sJ, P, un.tile, i * kFocusThreads + tid);
+                if (unit_pixel_ok<SKIP_ZERO>(px, P)) out[px] = a[i];
+            }
+        };
         int cur_chunk = -1;
         bool timed_out = false;
 
@@ -304,7 +316,11 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                                     tol, half_bw, inv_bw, taper, az_a, rh[i], rl[i], w[i]);
                         live |= w[i] != 0.0f;
                     }
-                    if (!__any_sync(0xffffffffu, live)) continue;
+                    if (!__any_sync(0xffffffffu, live)) {
+                        if (STORE) store_sums(c, make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                                              make_float2(0.f, 0.f));
+                        continue;
+                    }
 #pragma unroll
                     for (int i = 0; i < kFocusPT; ++i) {
                         chirp_phasors(rh[i], rl[i], g0h, g0l, g1, g1l, w[i], p[i], ql[i], q0[i]);
@@ -347,7 +363,11 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                         q0[i] = make_float2(w * ca, w * sa);
                         h[i] = make_float2(0.f, 0.f);
                     }
-                    if (SKIP_ZERO && !__any_sync(0xffffffffu, live)) continue;
+                    if (SKIP_ZERO && !__any_sync(0xffffffffu, live)) {
+                        if (STORE) store_sums(c, make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                                              make_float2(0.f, 0.f));
+                        continue;
+                    }
                 }
 
                 // Horner over blocks, last block first.
@@ -360,6 +380,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     for (int i = 0; i < kFocusPT; ++i) h[i] = horner_block(h[i], ql[i], p[i], xv);
                 }
 
+                if (STORE) store_sums(c, h[0], h[1], h[2], h[3]);
 #pragma unroll
                 for (int i = 0; i < kFocusPT; ++i) {
                     const float2 v = cmul(q0[i], h[i]);
@@ -660,33 +681,29 @@ int focus_fp32_smem_bytes(int stage_bytes)
 int focus_fp32_blocks_per_sm(int stage_bytes)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    int blocks = 0, blocks_skip = 0;
-    if (allow_max_dynamic_smem(focus_fp32_kernel<false>) != cudaSuccess ||
-        allow_max_dynamic_smem(focus_fp32_kernel<true>) != cudaSuccess)
-        return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel<false>, kFocusThreads, smem) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_skip, focus_fp32_kernel<true>, kFocusThreads, smem) !=
-            cudaSuccess)
-        return 0;
-    return blocks < blocks_skip ? blocks : blocks_skip;
+    int best = 1 << 30;
+    for (auto fn : {focus_fp32_kernel<false, false>, focus_fp32_kernel<true, false>, focus_fp32_kernel<false, true>,
+                    focus_fp32_kernel<true, true>}) {
+        int blocks = 0;
+        if (allow_max_dynamic_smem(fn) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kFocusThreads, smem) != cudaSuccess)
+            return 0;
+        best = blocks < best ? blocks : best;
+    }
+    return best;
 }
 
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
-                              int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero, cudaStream_t st)
+                              int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero, bool store_sums,
+                              cudaStream_t st)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes);
-    if (skip_zero) {
-        cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel<true>);
-        if (e != cudaSuccess) return e;
-        focus_fp32_kernel<true><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
-                                                                         status_dev, stage_bytes);
-    } else {
-        cudaError_t e = allow_max_dynamic_smem(focus_fp32_kernel<false>);
-        if (e != cudaSuccess) return e;
-        focus_fp32_kernel<false><<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev,
-                                                                          status_dev, stage_bytes);
-    }
+    using Fn = void (*)(const FocusJob *, const FocusUnit *, int, int *, int *, int);
+    const Fn fn = skip_zero ? (store_sums ? focus_fp32_kernel<true, true> : focus_fp32_kernel<true, false>)
+                            : (store_sums ? focus_fp32_kernel<false, true> : focus_fp32_kernel<false, false>);
+    cudaError_t e = allow_max_dynamic_smem(fn);
+    if (e != cudaSuccess) return e;
+    fn<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev, status_dev, stage_bytes);
     return cudaGetLastError();
 }
 

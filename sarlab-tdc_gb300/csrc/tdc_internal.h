@@ -88,6 +88,8 @@ struct FocusJob {
     const float *gsam;       // [s_pad] 2 f_s / c0 [cycles / m] (wide variants) or 2 pi x that [rad / m]
                              // (narrow variants) (FP32 general kernel, per-sample positions)
     float4 *partial;         // [n_groups][P]: (sum.re, sum.im, comp.re, comp.im)
+    float2 *chirp_sums;      // [C][P] per-(chirp, pixel) sums A = sum_s x_s z^s: written by the storing
+                             // focus instance, read by the adjoint that uses them (else null)
     long long P;
     int C;
     int S;
@@ -159,9 +161,10 @@ cudaError_t launch_focus_fp32_seg(const FocusJob *jobs_dev, const FocusUnit *uni
                                   cudaStream_t st);
 int focus_fp32_seg_blocks_per_sm(int stage_bytes);
 // skip_zero: skip chirps whose window is zero for a whole warp (any job with a finite band).
+// store_sums: also write job.chirp_sums (whole-row staging only).
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,
-                              bool skip_zero, cudaStream_t st);
+                              bool skip_zero, bool store_sums, cudaStream_t st);
 // Plain FP64-phase focus (comparator and general fallback), one CTA per unit.
 cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *status_dev, int per_sample, cudaStream_t st);
@@ -179,12 +182,16 @@ int focus_general_blocks_per_sm(int variant, int stage_bytes);
 int focus_general_smem_bytes(int stage_bytes);
 
 // Adjoint of the FP32-bulk focus w.r.t. per-chirp position offsets: per-(tile, chirp)
-// float4 partials, then an FP64 sum over tiles into grad[C][3].
+// float4 partials, then an FP64 sum over tiles into grad[C][3]. stored: job.xw holds the
+// rows pre-scaled by the sample index and job.chirp_sums the forward's per-(chirp, pixel)
+// sums (flat tiles).
 cudaError_t launch_adjoint_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
                                 int *status_dev, int stage_bytes, int stage_chirps, int grid_ctas,
-                                const float2 *gimg, float4 *gpart, cudaStream_t st);
+                                const float2 *gimg, float4 *gpart, bool stored, cudaStream_t st);
 cudaError_t launch_adjoint_reduce(const float4 *gpart, int n_tiles, int C, double *grad, cudaStream_t st);
-int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps);
+int adjoint_fp32_blocks_per_sm(int stage_bytes, int stage_chirps, bool stored);
+// rows_out[c][s] = s * rows[c][s] (complex, [C][s_pad]): the adjoint's pre-scaled rows.
+cudaError_t launch_scale_rows(const float2 *rows, int C, int s_pad, float2 *rows_out, cudaStream_t st);
 int adjoint_fp32_smem_bytes(int stage_bytes, int stage_chirps);
 
 // Let `fn` launch with as much dynamic shared memory as the device allows. The attribute

@@ -100,6 +100,17 @@ __global__ void rows_differ_vec_kernel(const uint4 *__restrict__ a4, unsigned in
     if (__syncthreads_or(differ) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
+// out[c][s] = s * rows[c][s]: rows pre-scaled by the sample index (the adjoint's B = sum_s s x_s z^s).
+__global__ void scale_rows_kernel(const float2 *__restrict__ rows, long long total, int s_pad, float2 *__restrict__ out)
+{
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const float s = (float)(idx % s_pad);
+        const float2 x = rows[idx];
+        out[idx] = make_float2(s * x.x, s * x.y);
+    }
+}
+
 // Bounding box of the grid's high floats: out = (min x, min y, min z, max x, max y, max z),
 // each as an order-preserving int (see float_key); out must start at (INT_MAX x3, INT_MIN x3).
 __device__ __forceinline__ int float_key(float f)
@@ -218,6 +229,16 @@ cudaError_t launch_rows_differ(const float *a, int C, int S, int k, int *flag, c
     long long blocks = (total + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     rows_differ_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const unsigned int *>(a), C, S, k, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale_rows(const float2 *rows, int C, int s_pad, float2 *rows_out, cudaStream_t st)
+{
+    const long long total = (long long)C * s_pad;
+    if (total <= 0) return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    scale_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(rows, total, s_pad, rows_out);
     return cudaGetLastError();
 }
 

@@ -162,6 +162,13 @@ struct tdc_processor {
     // FP32 general path: sample-0 records per chirp (when chirps holds one per sample),
     // per-sample offsets / windows, residual frequency table.
     tdc::impl::DevBuf gen_rec, traj, wins, wdot, gres;
+    // Autofocus: the forward's per-(chirp, pixel) sums and the rows pre-scaled by the sample
+    // index, so the adjoint computes only the index-weighted sums (keep_sums on).
+    tdc::impl::DevBuf chirp_sums, xs_scaled;
+    bool keep_sums = false;
+    bool xs_scaled_ready = false;
+    uint64_t state_epoch = 1;  // bumped when the prepared acquisition, its trajectory or the grid change
+    uint64_t sums_epoch = 0;   // state_epoch of the focus that wrote chirp_sums (0: none)
 
     // Device grid.
     long long P = 0;
@@ -196,6 +203,7 @@ struct tdc_processor {
     {
         return {&xw,      &chirps,     &skip,    &gs,      &pos_base, &wr,      &offsets,     &flag,     &gen_rec,
                 &traj,    &wins,       &wdot,    &gres,    &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch,
+                &chirp_sums, &xs_scaled,
                 &image_dev};
     }
 };

@@ -376,7 +376,7 @@ void tdc_server::launch_batch()
     unsigned char *d = static_cast<unsigned char *>(b.dev.p);
     err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
                              reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
-                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, st) != cudaSuccess;
+                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, false, st) != cudaSuccess;
     err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess;
     stats.launches++;
     if (!b.finishing.empty() && batches[bi ^ 1].in_flight) {

@@ -25,7 +25,8 @@ import _sarlabtdc
 class FocusOperator:
     """A processor with its acquisition and grid resident on the device."""
 
-    def __init__(self, proc: _sarlabtdc.TdcProcessor, start_args=(0.0, float("inf"), False, False, True)):
+    def __init__(self, proc: _sarlabtdc.TdcProcessor, start_args=(0.0, float("inf"), False, False, True),
+                 keep_sums: bool = True):
         self.proc = proc
         proc.prepare(*start_args)
         proc.uploadGrid()
@@ -33,15 +34,27 @@ class FocusOperator:
             raise RuntimeError("autofocus needs the FP32-bulk path (per-chirp trajectory, uniform sampling)")
         self.n_pix = proc.numPixels()
         self.n_pri = proc.numChirps()
+        # the forward keeps its per-chirp sums, so the adjoint recomputes only half
+        proc.keepChirpSums(keep_sums)
+        self._offsets = None  # offsets the resident trajectory was last set to
+
+    def _set_offsets(self, offsets: torch.Tensor | None):
+        o = None if offsets is None else offsets.detach().contiguous()
+        same = (o is None and self._offsets is None) or (
+            o is not None and self._offsets is not None and torch.equal(o, self._offsets))
+        if not same:
+            self.proc.setChirpOffsetsDevice(o)
+            self._offsets = None if o is None else o.clone()
 
     def image(self, offsets: torch.Tensor | None) -> torch.Tensor:
-        self.proc.setChirpOffsetsDevice(None if offsets is None else offsets.detach().contiguous())
+        self._set_offsets(offsets)
         img = torch.empty(self.n_pix, dtype=torch.complex64, device="cuda")
         self.proc.focusDevice(img)
         return img
 
     def adjoint(self, offsets: torch.Tensor, grad_image: torch.Tensor) -> torch.Tensor:
-        self.proc.setChirpOffsetsDevice(offsets.detach().contiguous())
+        # the forward's offsets are usually still set: the kept sums then stay valid
+        self._set_offsets(offsets)
         g = torch.empty((self.n_pri, 3), dtype=torch.float64, device="cuda")
         self.proc.adjointDevice(grad_image.detach().to(torch.complex64).contiguous(), g)
         return g
