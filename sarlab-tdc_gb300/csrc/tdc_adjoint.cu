@@ -33,6 +33,10 @@ namespace {
 
 constexpr int kLA = 4;  // in-block table length of the coupled recurrence (two tables per pixel)
 constexpr int kLS = 8;  // in-block table length with stored sums (one table, as in the forward)
+#ifndef TDC_ADJOINT_UNROLL
+#define TDC_ADJOINT_UNROLL 8
+#endif
+constexpr int kAdjUnroll = TDC_ADJOINT_UNROLL;  // Horner blocks unrolled in the stored-sums recurrence
 
 struct AdjShared {
     float t[kFocusPT * 6][kFocusThreads];  // pixel coordinates (hi xyz, lo xyz)
@@ -221,6 +225,7 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
 
                 if (STORED) {
                     // B = sum_s x'_s z^s over the pre-scaled rows, the forward's recurrence
+#pragma unroll kAdjUnroll
                     for (int b = nb - 1; b >= 0; --b) {
                         float4 xv[kLS / 2];
 #pragma unroll
