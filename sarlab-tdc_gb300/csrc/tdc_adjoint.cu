@@ -37,6 +37,10 @@ constexpr int kLS = 8;  // in-block table length with stored sums (one table, as
 #define TDC_ADJOINT_UNROLL 8
 #endif
 constexpr int kAdjUnroll = TDC_ADJOINT_UNROLL;  // Horner blocks unrolled in the stored-sums recurrence
+#ifndef TDC_ADJOINT_UNROLL_COUPLED
+#define TDC_ADJOINT_UNROLL_COUPLED 4
+#endif
+constexpr int kAdjUnrollCoupled = TDC_ADJOINT_UNROLL_COUPLED;  // ... and in the coupled one
 
 struct AdjShared {
     float t[kFocusPT * 6][kFocusThreads];  // pixel coordinates (hi xyz, lo xyz)
@@ -255,6 +259,7 @@ __global__ void __launch_bounds__(kFocusThreads, 3)
                         A[i] = px < P ? sums[(size_t)c * P + px] : make_float2(0.f, 0.f);
                     }
                 }
+#pragma unroll kAdjUnrollCoupled
                 for (int b = STORED ? -1 : nb - 1; b >= 0; --b) {
                     const float4 xa = xs[b * 2], xb = xs[b * 2 + 1];
                     const float xr[kLA] = {xa.x, xa.z, xb.x, xb.z};
