@@ -866,8 +866,10 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 
     const int tile_cols = choose_tile_cols(p);
     const long long n_tiles = tile_count(P, tile_cols, p->cols);
+    // (block tiles also depend on the grid's shape, not only on its pixel count)
+    const int plan_cols = tile_cols ? p->cols : 0;
     if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
-        max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols) {
+        max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols || plan_cols != p->plan_cols) {
         plan_groups(n_tiles, C, slots, p->plan_groups, p->plan_cpg,
                     path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot);
         if (max_unit_work > 0) {
@@ -880,6 +882,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         }
         p->plan_unit_cap = max_unit_work;
         p->plan_tile_cols = tile_cols;
+        p->plan_cols = plan_cols;
         p->units_host.clear();
         p->units_host.reserve((size_t)(n_tiles * p->plan_groups));
         for (long long t = 0; t < n_tiles; ++t)

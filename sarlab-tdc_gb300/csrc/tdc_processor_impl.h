@@ -182,7 +182,8 @@ struct tdc_processor {
     tdc::impl::DevBuf scratch;
     std::vector<tdc::FocusUnit> units_host;
     long long plan_P = -1;
-    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0, plan_tile_cols = -1;
+    int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0, plan_tile_cols = -1,
+        plan_cols = -1;
     double plan_unit_cap = 0.0;
     bool plan_uploaded = false;
 

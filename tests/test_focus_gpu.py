@@ -574,3 +574,26 @@ def test_block_tiles_under_a_finite_band(cuda_device, general):
     img_inf, stats_inf, _ = run_engine(api, sc.grid, (0.0, INF, False, True, True))
     assert stats_inf["tile_cols"] == 0
     _check(img_inf, full)
+
+
+def test_block_tiles_follow_a_new_grid_of_the_same_size(cuda_device):
+    """One processor, two grids with the same pixel count but different shapes (100 x 40
+    and 40 x 100) under a finite band: the block tiling is re-planned for the second grid
+    (a different number of tiles), and both images match the oracle."""
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=94, n_pri=300, n_samples=32, nx=40, ny=100, rail_len=0.3, device="cuda")
+    api = _moving_api(sc, speed=0.08)
+    args = (0.0, 14.0, False, True, True)
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                 api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+    for nx, ny in ((40, 100), (100, 40)):
+        grid = np.ascontiguousarray(scenes.ground_grid(nx, ny, 2e-3, y0=0.12).astype(np.float32))
+        p.setFocusGrid(grid)
+        p.start(*args)
+        img = p.getFocusedImage()
+        assert img.shape == (ny, nx)
+        assert p.lastStats()["tile_cols"] == 16
+        ref = _oracle(api, grid, args).reshape(img.shape)
+        _check(img, ref, l2=2e-4, phase=None)
