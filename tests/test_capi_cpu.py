@@ -196,3 +196,28 @@ def test_device_buffers_are_checked_before_any_kernel_writes_them():
     with pytest.raises(ValueError):
         S._device_buffer(np.zeros(100, np.complex64), "complex64", 100, "image")  # host array
     assert S._device_buffer(Fake((7, 3), "<f8"), "float64", 21, "offsets") == 0x1000
+
+
+def test_kernels_compile_without_register_spills(engine_lib):
+    """ptxas resource report of the build (sarlab-tdc_gb300/_build/ptxas.log): every
+    focus, adjoint and general-kernel instance fits its registers (no spill stores or
+    loads, <= 168 registers for 3 CTAs of 128 threads), so a change that pushes a hot
+    loop into local memory fails here, before it reaches a GPU."""
+    import re
+
+    log = (ROOT / "sarlab-tdc_gb300" / "_build" / "ptxas.log").read_text()
+    blocks = re.split(r"ptxas info\s*: Compiling entry function '", log)[1:]
+    seen = {}
+    for b in blocks:
+        name = b.split("'", 1)[0]
+        m_sp = re.search(r"(\d+) bytes spill stores, (\d+) bytes spill loads", b)
+        m_rg = re.search(r"Used (\d+) registers", b)
+        assert m_sp and m_rg, name
+        seen[name] = (int(m_sp.group(1)), int(m_sp.group(2)), int(m_rg.group(1)))
+    hot = {n: v for n, v in seen.items()
+           if any(k in n for k in ("focus_fp32", "focus_general", "adjoint_fp32_kernel", "focus_fp64"))}
+    # 4 bulk + 2 segmented + 7 general + 2 FP64 + 2 adjoint instances
+    assert len(hot) >= 17, sorted(hot)
+    for name, (st, ld, regs) in hot.items():
+        assert st == 0 and ld == 0, f"{name}: {st} B spill stores, {ld} B spill loads"
+        assert regs <= 168 or "focus_fp64" in name, f"{name}: {regs} registers"
