@@ -221,3 +221,11 @@ def test_kernels_compile_without_register_spills(engine_lib):
     for name, (st, ld, regs) in hot.items():
         assert st == 0 and ld == 0, f"{name}: {st} B spill stores, {ld} B spill loads"
         assert regs <= 168 or "focus_fp64" in name, f"{name}: {regs} registers"
+
+
+def test_integration_notes_cover_every_entry_point():
+    """INTEGRATION.md maps each C entry point to the reference interface it replaces (or
+    says it has none): every function the headers declare is listed there."""
+    text = (ROOT / "INTEGRATION.md").read_text()
+    missing = sorted(n for n in _declared_c_functions() if n not in text)
+    assert not missing, missing
