@@ -229,3 +229,14 @@ def test_integration_notes_cover_every_entry_point():
     text = (ROOT / "INTEGRATION.md").read_text()
     missing = sorted(n for n in _declared_c_functions() if n not in text)
     assert not missing, missing
+
+
+def test_bench_command_line_parses():
+    """bench.py loads and lists its options without a GPU (its arms and configs)."""
+    import sys
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--help"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    for opt in ("--gpus", "--steps", "--warmup", "--impl", "--config"):
+        assert opt in r.stdout
