@@ -61,7 +61,9 @@ def parse():
     ap.add_argument("--chirps", type=int, default=4096, help="config 2")
     ap.add_argument("--samples", type=int, default=1024, help="config 2")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
-    ap.add_argument("--quick", action="store_true", help="skip plain / e2e / CPU legs")
+    ap.add_argument("--quick", action="store_true", help="skip plain / e2e / CPU / serving / autofocus legs")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-mix leg of the default run")
+    ap.add_argument("--no-autofocus", action="store_true", help="skip the autofocus leg of the default run")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the oracle accuracy check")
     ap.add_argument("--general-only", action="store_true",
                     help="config 2 scene: only the FP32 vs FP64 general-kernel leg (per-sample trajectory)")
@@ -146,6 +148,12 @@ def workload(args, sc):
         return (f"precision study: {args.side}x{args.side} px @1mm, {sc.n_pri} chirps x {sc.n_samples} samples, "
                 "2 m jittered rail, FP64 positions + grid")
     return WORKLOADS[args.config]
+
+
+def bench_config(args, sc):
+    """The workload record, the same object in both arms."""
+    return {"workload": workload(args, sc), "pixels": sc.n_pix, "chirps": sc.n_pri, "samples": sc.n_samples,
+            "l2": "GPU arm: a 256 MiB buffer is written between timed steps (L2 is 129 MB)"}
 
 
 def make_scene(args, device):
@@ -335,9 +343,8 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
-           "config": {"workload": workload(args, sc),
-                      "pixels": P, "chirps": Cn, "samples": S, "correlations_per_step": corr,
-                      "l2": "256 MiB buffer written between timed steps", "path": path},
+           "config": bench_config(args, sc),
+           "run": {"correlations_per_step": corr, "path": path},
            "latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 3),
                           "p99": round(float(np.percentile(step_ms, 99)), 3)},
            "gpu_launches": 2 * args.steps, "clocks": clk, "roofline": roofline}
@@ -428,6 +435,12 @@ def run_ours(args):
                                "sample": f"{npx} random pixels x {Cn} chirps x {S} samples ({dt:.1f}s), "
                                          "FP64 OpenMP oracle loop"}
         log(f"cpu {out['cpu_baseline']}")
+        del p
+        torch.cuda.empty_cache()
+        if not args.no_serving:
+            out["serving"] = serving_leg(args)
+        if not args.no_autofocus:
+            out["autofocus"] = autofocus_leg(args)
     print(json.dumps(out), flush=True)
 
 
@@ -556,9 +569,10 @@ def run_general_only(args):
     print(json.dumps(out), flush=True)
 
 
-def run_serving(args):
+def serving_leg(args):
     """Config 4: a seeded Poisson stream of focus requests through the request loop, against
-    the same jobs run one after another through the processor (FIFO, same arrival times)."""
+    the same jobs run one after another through the processor (FIFO, same arrival times).
+    Returns the `serving` object (with the clocks sampled while both ran)."""
     import threading
 
     from sarlabtdc import scenes
@@ -591,6 +605,8 @@ def run_serving(args):
         f"{sum(j['corr'] for j in jobs) / 1e12:.1f} Tcorr total")
     start = (0.0, float("inf"), False, False, True)
 
+    clocks = Clocks()
+    clocks.start()
     # request loop
     with FocusServer(max_jobs=16) as srv:
         ids = [None] * n
@@ -628,23 +644,36 @@ def run_serving(args):
         finish = max(finish, a) + sv
         lat_s.append(finish - a)
     lat_s = np.array(lat_s) * 1e3
+    clk = clocks.stop()
     serial = {"p50_ms": round(float(np.percentile(lat_s, 50)), 1), "p99_ms": round(float(np.percentile(lat_s, 99)), 1),
               "gcorr_s": round(total / (finish - arrivals[0]) / 1e9, 1), "span_s": round(finish - arrivals[0], 2)}
     log(f"serial: {serial}")
+    return {"workload": f"serving mix: {n} requests, Poisson {args.rate}/s, grids 128^2..2048^2, "
+                        "256..8192 chirps (log-uniform), 256/512/1024 samples, 1-100 targets",
+            "unit": UNIT, "total_correlations": total, "request_loop": served, "serial_processor": serial,
+            "offered_gcorr_s": round(total / (arrivals[-1] - arrivals[0]) / 1e9, 1),
+            "serial_how": "the same jobs one at a time through a one-slot request loop, FIFO on the same arrivals "
+                          "(latency = queueing on those arrivals + measured service time)",
+            "clocks": clk}
+
+
+def run_serving(args):
+    """Config 4 alone: one JSON line."""
+    sv = serving_leg(args)
+    served = sv["request_loop"]
     out = {"metric": "serving: p50/p99 focus latency and aggregate Gcorr/s", "value": served["gcorr_s"],
            "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
            "data": "synthetic (seeded Poisson arrivals, point targets)",
-           "config": {"workload": f"serving mix: {n} requests, Poisson {args.rate}/s, grids 128^2..2048^2, "
-                                  "256..8192 chirps (log-uniform), 256/512/1024 samples, 1-100 targets",
-                      "total_correlations": total},
+           "config": {"workload": sv["workload"], "total_correlations": sv["total_correlations"]},
            "latency_ms": {"p50": served["p50_ms"], "p99": served["p99_ms"]},
-           "request_loop": served, "serial_processor": serial,
-           "offered_gcorr_s": round(total / (arrivals[-1] - arrivals[0]) / 1e9, 1)}
+           "request_loop": served, "serial_processor": sv["serial_processor"],
+           "offered_gcorr_s": sv["offered_gcorr_s"], "clocks": sv["clocks"]}
     print(json.dumps(out), flush=True)
 
 
-def run_autofocus(args):
-    """Config 5: entropy autofocus of a random-walk trajectory error through the adjoint kernel."""
+def autofocus_leg(args):
+    """Config 5: entropy autofocus of a random-walk trajectory error through the adjoint kernel.
+    Returns the `autofocus` object (with the clocks sampled while it ran)."""
     import torch
 
     import _sarlabtdc
@@ -659,6 +688,8 @@ def run_autofocus(args):
     p.setFocusGridF64(sc.grid)
     op = autofocus.FocusOperator(p, (0.0, float("inf"), False, False, True))
     corr = sc.correlations()
+    clocks = Clocks()
+    clocks.start()
     # timing of forward and adjoint
     zero = torch.zeros((sc.n_pri, 3), dtype=torch.float64, device="cuda")
     g = torch.randn(op.n_pix, dtype=torch.complex64, device="cuda")
@@ -724,23 +755,34 @@ def run_autofocus(args):
     res = autofocus.autofocus(op, steps=args.af_steps, lr=args.af_lr)
     ph1 = autofocus.residual_phase_rms(res.offsets.cpu().numpy(), walk, sc.positions, centre, lam)
     coh1 = autofocus.coherence(op.image(res.offsets).cpu().numpy(), ideal)
-    out = {"metric": "autofocus: adjoint accuracy, entropy, residual phase, time per Adam step",
-           "value": round(float(np.median(res.step_ms)), 2), "unit": "ms/Adam step (median)", "higher_is_better": False,
+    clk = clocks.stop()
+    out = {"workload": "autofocus: 512x512 px @1mm, 4096 chirps x 1024 samples over 2 m, random walk 0.2 mm/step",
+           "correlations_per_forward": corr,
            "step_ms": {"p50": round(float(np.median(res.step_ms)), 2), "mean": round(float(np.mean(res.step_ms)), 2),
                        "max": round(float(np.max(res.step_ms)), 2)},
-           "n_gpus": 1, "dtype": "f32",
-           "data": "synthetic (seeded random-walk trajectory error, 30 targets)",
-           "config": {"workload": "autofocus: 512x512 px @1mm, 4096 chirps x 1024 samples over 2 m, random walk "
-                                  "0.2 mm/step", "correlations_per_forward": corr},
            "forward_ms": round(fwd_ms, 2), "adjoint_ms": round(adj_ms, 2), "adjoint_read_kept_sums": adj_kept,
            "adjoint_recomputing_ms": round(adj_full_ms, 2),
            "forward_gcorr_s": round(corr / (fwd_ms / 1e3) / 1e9, 1),
            "adjoint_gcorr_s": round(corr / (adj_ms / 1e3) / 1e9, 1),
-           "gradient_vs_fp64_oracle_rel_l2": grad_err, "gradient_vs_central_fd_h1e-6_rel": fd_rel,
+           "gradient_vs_fp64_oracle_rel_l2": grad_err, "gradient_pixels": int(pix.size),
+           "gradient_vs_central_fd_h1e-6_rel": fd_rel,
            "entropy": {"start": res.entropy[0], "end": res.entropy[-1]},
            "residual_phase_rms_rad": {"start": ph0, "end": ph1},
            "coherence_with_true_trajectory_image": {"start": coh0, "end": coh1},
-           "adam_steps": args.af_steps, "lr_m": args.af_lr}
+           "adam_steps": args.af_steps, "lr_m": args.af_lr, "clocks": clk}
+    del op, p
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_autofocus(args):
+    """Config 5 alone: one JSON line."""
+    af = autofocus_leg(args)
+    out = {"metric": "autofocus: adjoint accuracy, entropy, residual phase, time per Adam step",
+           "value": af["step_ms"]["p50"], "unit": "ms/Adam step (median)", "higher_is_better": False,
+           "n_gpus": 1, "dtype": "f32", "data": "synthetic (seeded random-walk trajectory error, 30 targets)",
+           "config": {"workload": af["workload"], "correlations_per_forward": af["correlations_per_forward"]},
+           **{k: v for k, v in af.items() if k not in ("workload", "correlations_per_forward")}}
     print(json.dumps(out), flush=True)
 
 
@@ -779,8 +821,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(times)), 2), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
            "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
-           "config": {"workload": workload(args, sc),
-                      "pixels": sc.n_pix, "chirps": sc.n_pri, "samples": sc.n_samples},
+           "config": bench_config(args, sc),
            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
                             "sample": f"{npx} random pixels per step x {sc.n_pri} chirps x {sc.n_samples} samples; "
                                       "the reference has no CPU focus path: FP64 OpenMP restatement of "

@@ -342,14 +342,18 @@ int tdc_selftest_wait_timeout(int device, int limit_us, int *timed_out, double *
  * tdc_processor_focus_device on inputs and an output the caller owns; its
  * scratch memory is a fixed array inside this library (TDC_NOALLOC_SCRATCH_BYTES
  * on every GPU that loads the library, held until the process exits), so it
- * calls no cudaMalloc / cudaFree. That limits the grid to about 2M pixels
- * (larger grids return TDC_ERR_UNSUPPORTED before anything runs).
+ * calls no cudaMalloc / cudaFree. That limits the grid to about 2M pixels, and
+ * rows to TDC_NOALLOC_MAX_SAMPLES samples (whole rows are staged; the processor
+ * stages longer rows in segments). Larger grids or rows return
+ * TDC_ERR_UNSUPPORTED before anything runs.
  *
  * All calls on a device share the one array: calls that overlap on the GPU
  * (other streams, other host threads) race on it and must be serialised by the
- * caller. The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture. tdc_focus_noalloc is blocking: it returns after the image
+ * caller. Each call outside stream capture looks up the array's device address
+ * (cudaGetSymbolAddress) in the current context, so a device reset between calls
+ * is harmless; a call under capture uses the address the last uncaptured call on
+ * that device found, so make one call on each device before any stream capture
+ * (and again after a device reset). tdc_focus_noalloc is blocking: it returns after the image
  * is written and the kernels' status word has been read (TDC_ERR_TIMEOUT when a
  * bounded wait in the focus kernel expired). tdc_focus_noalloc_async enqueues the
  * same kernels and a copy of the status word into status_dev (a device int,
@@ -373,6 +377,10 @@ int tdc_selftest_wait_timeout(int device, int limit_us, int *timed_out, double *
  * Output: image_dev, n_pix complex floats (interleaved).
  */
 #define TDC_NOALLOC_SCRATCH_BYTES (32u << 20)
+/* Largest n_samples tdc_focus_noalloc takes: three pipeline stages of one whole row
+ * (n_samples rounded up to 16, 8 bytes a sample, plus a 48-byte record) within the
+ * shared memory a block may use. */
+#define TDC_NOALLOC_MAX_SAMPLES 9104
 
 typedef struct tdc_noalloc_focus_args {
     const float *samples;

@@ -47,6 +47,7 @@ class NoallocFocusArgs(C.Structure):
 
 
 NOALLOC_SCRATCH_BYTES = 32 << 20
+NOALLOC_MAX_SAMPLES = 9104
 
 
 class JobDesc(C.Structure):

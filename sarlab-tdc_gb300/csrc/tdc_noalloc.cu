@@ -22,6 +22,7 @@
 
 #include "tdc_gb300.h"
 #include "tdc_internal.h"
+#include "tdc_processor_impl.h"
 
 using namespace tdc;
 
@@ -31,7 +32,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TDC_NOALLOC_SCR
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-unsigned char *g_scratch_addr[kMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+// Device address of g_noalloc_scratch per device, as last looked up with that device
+// current. Calls outside stream capture look it up again (cheap), so a device reset or
+// another context made current since is picked up; calls under capture use this copy.
+unsigned char *g_scratch_addr[kMaxDevices] = {};
 
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -128,26 +132,35 @@ int enqueue(const tdc_noalloc_focus_args *a, float *image_dev, cudaStream_t st, 
                                              "holds " + std::to_string((size_t)TDC_NOALLOC_SCRATCH_BYTES) +
                                              " (about 2M pixels)");
     }
-    const int row = s_pad * 8 + (int)sizeof(ChirpRec);
-    const int cb = std::max(1, 16640 / row);
-    const int stage_bytes = (int)round_up((size_t)cb * row, 128);
-    if (focus_fp32_smem_bytes(stage_bytes) > 227 * 1024)
-        return fail(TDC_ERR_UNSUPPORTED, "tdc_focus_noalloc: nSamples too large for the shared-memory stages");
+    // Whole rows only (the processor stages longer rows in segments): the same limit as
+    // the processor's choice between the two, TDC_NOALLOC_MAX_SAMPLES samples.
+    if (impl::needs_segments(s_pad))
+        return fail(TDC_ERR_UNSUPPORTED, "tdc_focus_noalloc: nSamples " + std::to_string(S) + " above " +
+                                             std::to_string(TDC_NOALLOC_MAX_SAMPLES) +
+                                             " (whole rows must fit the shared-memory stages)");
+    int cb = 1;
+    const int stage_bytes = impl::stage_bytes_for(s_pad, cb);
 
     // ---- per-device set-up: the device address of the scratch array ----
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(TDC_ERR_UNSUPPORTED, "device index out of range");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
     unsigned char *base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch_addr[dev]) {
+        if (cap == cudaStreamCaptureStatusNone) {
             void *ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess || !ptr)
                 return fail(TDC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             g_scratch_addr[dev] = static_cast<unsigned char *>(ptr);
+        } else if (!g_scratch_addr[dev]) {
+            return fail(TDC_ERR_UNSUPPORTED, "tdc_focus_noalloc: the first call on a device must come before "
+                                             "any stream capture (it looks up the scratch array's address)");
         }
         base = g_scratch_addr[dev];
     }

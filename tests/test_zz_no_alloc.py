@@ -11,7 +11,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from tdc_testutil import max_phase_err, rel_l2, run_engine
+import oracle
+from tdc_testutil import max_phase_err, problem_from_api, rel_l2, run_engine
 
 L2_TOL = 1e-4
 PHASE_TOL = 1e-3
@@ -104,6 +105,180 @@ def test_noalloc_focus_matches_device_focus_twice_in_a_row(cuda_device):
         assert rel_l2(o, ref_np) <= L2_TOL
         assert max_phase_err(o, ref_np) <= PHASE_TOL
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def _split(a):
+    """Double-float pair (high, low) of an FP64 array as float32 arrays."""
+    hi = np.asarray(a, np.float64).astype(np.float32)
+    lo = (np.asarray(a, np.float64) - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
+
+
+def _skip_table(api, centre):
+    """The documented skip-point layout, ceil(n_pri / 128) x 9 points x 8 floats (position xyz,
+    window centre, velocity xyz, 0), at the reference's 3 x 3 (PRI, sample) points of each
+    chunk -- stale staging rows of a partial last chunk included (tdcprocessor.cpp:347-383)."""
+    n_pri, S = api["rawData"].shape
+    chunk = 128
+    rows, samples = oracle.skip_points(S, chunk)
+    n_chunks = (n_pri + chunk - 1) // chunk
+    tab = np.zeros((n_chunks, 9, 8), np.float32)
+    for k in range(n_chunks):
+        for i in range(3):
+            pri = oracle.skip_row_pri(n_pri, chunk, k, rows[i])
+            for j in range(3):
+                tab[k, i * 3 + j, 3] = centre
+                if pri >= 0:
+                    tab[k, i * 3 + j, 0:3] = api["position"][pri, samples[j]]
+                    tab[k, i * 3 + j, 4:7] = api["velocity"][pri, samples[j]]
+    return tab
+
+
+def _noalloc_args(api, grid, torch, pos64=None, grid64=None, centre=0.0, band=float("inf"), taper=True,
+                  skip=False):
+    """Arguments and caller-owned device buffers of one tdc_focus_noalloc call."""
+    import _tdc_capi
+
+    samples, chirps, grid_hi, g0, g1, lam = _device_inputs(api, grid, torch)
+    rec = chirps.cpu().numpy()
+    rec[:, 3] = np.float32(centre)
+    keep = []
+    if pos64 is not None:
+        hi, lo = _split(pos64)
+        rec[:, 0:3] = hi
+        rec[:, 4:7] = lo
+    chirps = torch.from_numpy(rec).cuda()
+    grid_lo = None
+    if grid64 is not None:
+        hi, lo = _split(np.asarray(grid64).reshape(-1, 3))
+        gh = np.zeros((hi.shape[0], 4), np.float32)
+        gl = np.zeros((hi.shape[0], 4), np.float32)
+        gh[:, :3], gl[:, :3] = hi, lo
+        grid_hi = torch.from_numpy(gh).cuda()
+        grid_lo = torch.from_numpy(gl).cuda()
+    skip_dev = torch.from_numpy(_skip_table(api, np.float32(centre))).cuda() if skip else None
+    keep += [samples, chirps, grid_hi, grid_lo, skip_dev]
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = samples.data_ptr()
+    a.chirps = chirps.data_ptr()
+    a.skip_points = None if skip_dev is None else skip_dev.data_ptr()
+    a.grid_hi = grid_hi.data_ptr()
+    a.grid_lo = None if grid_lo is None else grid_lo.data_ptr()
+    a.n_pix = grid_hi.shape[0]
+    a.n_pri, a.n_samples = api["rawData"].shape
+    a.g0, a.g1 = g0, g1
+    a.lambda_ = lam
+    a.doppler_bandwidth = float(band)
+    a.doppler_win_taper = int(bool(taper))
+    return a, keep
+
+
+def _noalloc_twice(a):
+    """Two calls in a row (the shared scratch keeps the first call's contents)."""
+    import torch
+
+    import _tdc_capi
+
+    lib = _tdc_capi.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for _ in range(2):
+        out = torch.full((a.n_pix,), complex(float("nan"), 0.0), dtype=torch.complex64, device="cuda")
+        rc = lib.tdc_focus_noalloc(C.byref(a), C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+        assert rc == 0, _tdc_capi.last_error()
+        outs.append(out.cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+    return outs[0]
+
+
+@pytest.mark.gpu
+def test_noalloc_plain_against_the_oracle(cuda_device):
+    import torch
+
+    from sarlabtdc import scenes
+
+    sc = scenes.small_scene(seed=63, n_pri=300, n_samples=100, nx=40, ny=30, device="cuda")
+    api = sc.api_arrays()
+    a, keep = _noalloc_args(api, sc.grid, torch)
+    got = _noalloc_twice(a)
+    ref = oracle.focus(problem_from_api(api, sc.grid), oracle.Opts(applyRangeWin=False))
+    assert rel_l2(got, ref) <= L2_TOL
+    assert max_phase_err(got, ref) <= PHASE_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("taper", [True, False])
+def test_noalloc_finite_band_and_skip_points_against_the_oracle(cuda_device, taper):
+    """Finite Doppler band (the instance that skips zero-window chirps) with the chunk skip
+    test from a caller-built skip table; 750 chirps, so the last chunk is partial and its
+    skip points read stale staging rows. The antenna moves along the rail, so the window
+    and the skip test cut real work."""
+    import torch
+
+    from sarlabtdc import scenes
+
+    sc = scenes.small_scene(seed=64, n_pri=750, n_samples=64, nx=21, ny=17, rail_len=0.75, device="cuda")
+    api = sc.api_arrays()
+    vel = np.zeros_like(api["velocity"])
+    vel[..., 0] = 0.05
+    api["velocity"] = vel
+    centre, band = 2.0, 18.0
+    a, keep = _noalloc_args(api, sc.grid, torch, centre=centre, band=band, taper=taper, skip=True)
+    got = _noalloc_twice(a)
+    prob = problem_from_api(api, sc.grid)
+    ref = oracle.focus(prob, oracle.Opts(dopplerWinCenter=centre, dopplerBandwidth=band, applyRangeWin=False,
+                                         dopplerWinTaper=taper, skip_test=True))
+    full = oracle.focus(prob, oracle.Opts(applyRangeWin=False, dopplerWinTaper=taper))
+    assert rel_l2(ref, full) > 0.05                      # the window does cut pixels' chirps
+    no_skip = oracle.focus(prob, oracle.Opts(dopplerWinCenter=centre, dopplerBandwidth=band, applyRangeWin=False,
+                                             dopplerWinTaper=taper, skip_test=False))
+    assert np.any(ref != no_skip)                        # and the skip test drops whole chunks
+    # chirps at the inclusive band edge may fall either side in FP32: L2 bound only
+    assert rel_l2(got, ref) <= 2e-4
+
+
+@pytest.mark.gpu
+def test_noalloc_double_float_positions_and_grid_against_the_oracle(cuda_device):
+    """FP64 positions and grid passed as double-float pairs (low floats in the chirp records
+    and grid_lo), against the oracle on the FP64 values."""
+    import torch
+
+    from sarlabtdc import scenes
+
+    sc = scenes.small_scene(seed=65, n_pri=512, n_samples=256, nx=24, ny=24, jitter=0.5e-3, spacing=1e-3,
+                            y0=0.6, rail_len=1.0, device="cuda")
+    api = sc.api_arrays()
+    a, keep = _noalloc_args(api, sc.grid, torch, pos64=sc.positions, grid64=sc.grid)
+    got = _noalloc_twice(a)
+    ref = oracle.focus(problem_from_api(api, sc.grid, pos64=sc.positions, grid64=True),
+                       oracle.Opts(applyRangeWin=False))
+    assert rel_l2(got, ref) <= L2_TOL
+    assert max_phase_err(got, ref) <= PHASE_TOL
+    # the low floats matter at this precision: the FP32-rounded inputs give a different image
+    a32, keep32 = _noalloc_args(api, sc.grid, torch)
+    assert rel_l2(_noalloc_twice(a32), ref) > rel_l2(got, ref)
+
+
+def test_noalloc_rejects_rows_longer_than_its_stages():
+    """Size check only: rows above TDC_NOALLOC_MAX_SAMPLES return TDC_ERR_UNSUPPORTED before
+    any CUDA call (run where no GPU is present)."""
+    import torch
+
+    import _tdc_capi
+
+    if torch.cuda.is_available():
+        pytest.skip("host-side rejection is checked where no GPU is present")
+    lib = _tdc_capi.lib()
+    a = _tdc_capi.NoallocFocusArgs()
+    a.samples = a.chirps = a.grid_hi = 4096      # never dereferenced: rejected on size first
+    a.n_pix = 512
+    a.n_pri = 128
+    a.n_samples = _tdc_capi.NOALLOC_MAX_SAMPLES + 1
+    a.lambda_ = 0.0039
+    a.doppler_bandwidth = float("inf")
+    rc = lib.tdc_focus_noalloc(C.byref(a), C.c_void_p(4096), None)
+    assert rc == _tdc_capi.TDC_ERR_UNSUPPORTED
+    assert "nSamples" in _tdc_capi.last_error()
 
 
 @pytest.mark.gpu
