@@ -142,7 +142,7 @@ typedef struct tdc_start_stats {
                              rows x tile_cols columns (finite Doppler band, antenna moving along the
                              grid's columns) */
     int adjoint_stored;   /* the last adjoint read the kept per-chirp sums (1) or recomputed them (0) */
-    int reserved;
+    int motion_segment;   /* smooth-motion path: samples per linearised segment; 0 on the other paths */
 } tdc_start_stats;
 
 typedef enum tdc_path {
@@ -150,8 +150,11 @@ typedef enum tdc_path {
     TDC_PATH_FP64_PHASE = 1,   /* comparator, per-chirp trajectory */
     TDC_PATH_GENERAL = 2,      /* per-sample trajectory / window or non-uniform sample times: FP32 phasors
                                   with a double-float range at sample 0 and per-sample corrections */
-    TDC_PATH_GENERAL_FP64 = 3  /* the same inputs with FP64 phase per sample (FP64 precision, or intra-chirp
+    TDC_PATH_GENERAL_FP64 = 3, /* the same inputs with FP64 phase per sample (FP64 precision, or intra-chirp
                                   motion too large for the FP32 correction) */
+    TDC_PATH_FP32_MOTION = 4   /* per-sample positions moving smoothly within each chirp (a quadratic in the
+                                  sample index to within their FP32 rounding), uniform sample spacing, one
+                                  window per chirp: the per-sample phase correction linearised per segment */
 } tdc_path;
 
 int tdc_processor_last_stats(const tdc_processor *proc, tdc_start_stats *out);
@@ -167,6 +170,11 @@ int tdc_range_window(float *w_dev, int n_samples, int apply_range_win, void *str
 /* Skip test of tdcprocessor.cpp:347-383 on (1, default) or off. Takes effect
  * at the next start() / prepare(). */
 int tdc_processor_set_skip_test(tdc_processor *proc, int enable);
+
+/* Smooth-motion path (TDC_PATH_FP32_MOTION) on (1, default) or off (0: such inputs take
+ * the FP32 general kernel). Extension without a reference counterpart; takes effect at the
+ * next focus. */
+int tdc_processor_set_motion_path(tdc_processor *proc, int enable);
 
 /*
  * The parts of start() before the per-pixel work, leaving the acquisition

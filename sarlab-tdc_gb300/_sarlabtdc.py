@@ -206,6 +206,11 @@ class TdcProcessor:
         code = {"fp32": _lib.PRECISION_FP32_BULK, "fp64": _lib.PRECISION_FP64_PHASE}[precision]
         _lib.check(_lib.lib().tdc_processor_set_precision(self._h, code))
 
+    def setMotionPath(self, enable: bool):
+        """Extension: per-sample positions that move smoothly within each chirp take the
+        smooth-motion kernel (default) or, when off, the FP32 general kernel."""
+        _lib.check(_lib.lib().tdc_processor_set_motion_path(self._h, int(bool(enable))))
+
     def setSkipTest(self, enable: bool):
         _lib.check(_lib.lib().tdc_processor_set_skip_test(self._h, int(bool(enable))))
 

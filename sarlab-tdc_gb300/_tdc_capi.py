@@ -24,7 +24,7 @@ TDC_ERR_SHAPE = -7
 PRECISION_FP32_BULK = 0
 PRECISION_FP64_PHASE = 1
 
-PATH_NAMES = {0: "fp32_bulk", 1: "fp64_phase", 2: "general", 3: "general_fp64"}
+PATH_NAMES = {0: "fp32_bulk", 1: "fp64_phase", 2: "general", 3: "general_fp64", 4: "fp32_motion"}
 
 
 class NoallocFocusArgs(C.Structure):
@@ -124,7 +124,7 @@ class StartStats(C.Structure):
         ("general_variant", C.c_int),
         ("tile_cols", C.c_int),
         ("adjoint_stored", C.c_int),
-        ("reserved", C.c_int),
+        ("motion_segment", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -156,6 +156,7 @@ SIGNATURES = [
     ("tdc_processor_last_stats", C.c_int, [_vp, C.POINTER(StartStats)]),
     ("tdc_range_window", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     ("tdc_processor_set_skip_test", C.c_int, [_vp, C.c_int]),
+    ("tdc_processor_set_motion_path", C.c_int, [_vp, C.c_int]),
     ("tdc_processor_prepare", C.c_int, [_vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]),
     ("tdc_processor_upload_grid", C.c_int, [_vp]),
     ("tdc_processor_focus_device", C.c_int, [_vp, _vp, _vp]),

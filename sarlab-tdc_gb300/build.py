@@ -23,8 +23,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libtdc_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["tdc_focus.cu", "tdc_general.cu", "tdc_fp64.cu", "tdc_prep.cu", "tdc_probe.cu", "tdc_noalloc.cu",
-              "tdc_adjoint.cu"]
+CU_SOURCES = ["tdc_focus.cu", "tdc_general.cu", "tdc_motion.cu", "tdc_fp64.cu", "tdc_prep.cu", "tdc_probe.cu",
+              "tdc_noalloc.cu", "tdc_adjoint.cu"]
 CPP_SOURCES = ["tdc_capi.cpp", "tdc_server.cpp"]
 
 

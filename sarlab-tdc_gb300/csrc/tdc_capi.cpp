@@ -86,6 +86,9 @@ constexpr double kUniformPhaseTolRad = 1e-4;
 constexpr double kGeneralMaxEps = 0.1;
 constexpr double kGeneralNarrowEps = 0.02;
 constexpr double kGeneralNarrowCycles = 4.0;
+// Smooth-motion kernel: largest deviation of the per-sample phase correction from its
+// per-segment linear model (chord + mean offset) [rad].
+constexpr double kMotionTolRad = 2e-3;
 #ifndef TDC_GENERAL_STAGE_TARGET
 #define TDC_GENERAL_STAGE_TARGET 32768
 #endif
@@ -384,6 +387,87 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         });
     }
 
+    // ---- smooth intra-chirp motion (the smooth-motion kernel) ----
+    // Least-squares fit of each chirp's D_s = P[c,s] - P[c,0] by V0 + V1 s + V2 s^2 (orthogonal
+    // polynomials in the centred index); accepted when every sample's residual stays within one
+    // ulp of the chirp's largest FP32 coordinate on that axis, i.e. what remains is the rounding
+    // of the input.
+    std::vector<MotionRec> mrecs;
+    p->motion_fit_ok = false;
+    p->motion_v1max = p->motion_v2max = 0.0;
+    if (p->traj_varies && !p->win_varies && S >= 3) {
+        mrecs.resize(C);
+        const double hs = 0.5 * (S - 1);
+        double sxx = 0.0, m2 = 0.0, sqq = 0.0;
+        for (int s = 0; s < S; ++s) m2 += (s - hs) * (s - hs);
+        m2 /= S;
+        for (int s = 0; s < S; ++s) {
+            const double x = s - hs, q = x * x - m2;
+            sxx += x * x;
+            sqq += q * q;
+        }
+        std::vector<double> vmax(3 * 16, 0.0);
+        std::vector<char> bad(16, 0);
+        const int nt = parallel_chirps(C, S, [&](int t, int cb, int ce) {
+            double v1m = 0.0, v2m = 0.0;
+            bool fail_fit = false;
+            for (int c = cb; c < ce && !fail_fit; ++c) {
+                const float *p0 = p->pos + 3 * ti(c, 0);
+                double V0[3], V1[3], V2[3];
+                for (int k = 0; k < 3; ++k) {
+                    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+                    for (int s = 0; s < S; ++s) {
+                        const double y = (double)p->pos[3 * ti(c, s) + k] - (double)p0[k];
+                        const double x = s - hs;
+                        a0 += y;
+                        a1 += y * x;
+                        a2 += y * (x * x - m2);
+                    }
+                    a0 /= S;
+                    a1 /= sxx;
+                    a2 /= sqq;
+                    V0[k] = a0 - a1 * hs + a2 * (hs * hs - m2);
+                    V1[k] = a1 - 2.0 * a2 * hs;
+                    V2[k] = a2;
+                    float vmag = 0.f;
+                    for (int s = 0; s < S; ++s) vmag = std::max(vmag, std::fabs(p->pos[3 * ti(c, s) + k]));
+                    const double ulp = vmag > 0.f ? std::ldexp(1.0, std::ilogb(vmag) - 23) : 1e-38;
+                    for (int s = 0; s < S && !fail_fit; ++s) {
+                        const double y = (double)p->pos[3 * ti(c, s) + k] - (double)p0[k];
+                        const double r = y - (V0[k] + s * (V1[k] + s * V2[k]));
+                        if (!(std::fabs(r) <= ulp)) fail_fit = true;
+                    }
+                }
+                if (fail_fit) break;
+                const ChirpRec r0 = make_record(p, c, 0, o.centroid != 0, o.center);
+                float h[3], l[3];
+                for (int k = 0; k < 3; ++k) split_dd((double)p0[k] + V0[k], h[k], l[k]);
+                MotionRec &m = mrecs[c];
+                const double n1 = std::sqrt(V1[0] * V1[0] + V1[1] * V1[1] + V1[2] * V1[2]);
+                const double n2 = std::sqrt(V2[0] * V2[0] + V2[1] * V2[1] + V2[2] * V2[2]);
+                m.p_hi = make_float4(h[0], h[1], h[2], r0.p_hi.w);
+                m.p_lo = make_float4(l[0], l[1], l[2], 0.f);
+                m.vel = make_float4(r0.vel.x, r0.vel.y, r0.vel.z,
+                                    (float)(2.0 * (V1[0] * V2[0] + V1[1] * V2[1] + V1[2] * V2[2])));
+                m.v1 = make_float4((float)V1[0], (float)V1[1], (float)V1[2], (float)(n1 * n1));
+                m.v2 = make_float4((float)V2[0], (float)V2[1], (float)V2[2], (float)(n2 * n2));
+                v1m = std::max(v1m, n1);
+                v2m = std::max(v2m, n2);
+            }
+            vmax[3 * t] = v1m;
+            vmax[3 * t + 1] = v2m;
+            bad[t] = fail_fit ? 1 : 0;
+        });
+        bool ok = true;
+        for (int t = 0; t < nt; ++t) {
+            ok = ok && !bad[t];
+            p->motion_v1max = std::max(p->motion_v1max, vmax[3 * t]);
+            p->motion_v2max = std::max(p->motion_v2max, vmax[3 * t + 1]);
+        }
+        p->motion_fit_ok = ok;
+        if (!ok) mrecs.clear();
+    }
+
     // ---- skip-test points (tdcprocessor.cpp:347-383, stale staging rows included) ----
     const int n_chunks = (C + kChunk - 1) / kChunk;
     std::vector<SkipPoint> skip((size_t)n_chunks * 9);
@@ -479,6 +563,13 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         TDC_CK(p->wins.ensure(wins.size() * sizeof(float4)), "alloc per-sample windows");
         TDC_CK(cudaMemcpyAsync(p->wins.p, wins.data(), wins.size() * sizeof(float4), cudaMemcpyHostToDevice, st),
                "copy per-sample windows");
+    }
+    if (!mrecs.empty()) {
+        TDC_CK(p->motion_rec.ensure(mrecs.size() * sizeof(MotionRec)), "alloc motion records");
+        TDC_CK(cudaMemcpyAsync(p->motion_rec.p, mrecs.data(), mrecs.size() * sizeof(MotionRec),
+                               cudaMemcpyHostToDevice, st),
+               "copy motion records");
+        p->stats.h2d_bytes += (int64_t)(mrecs.size() * sizeof(MotionRec));
     }
     if (!wdot.empty()) {
         TDC_CK(p->wdot.ensure(wdot.size() * sizeof(float)), "alloc per-sample window offsets");
@@ -611,6 +702,40 @@ int general_variant(const tdc_processor *p)
     return (p->traj_varies ? 1 : 0) | (p->win_varies ? 2 : 0) | (wide ? 4 : 0);
 }
 
+int motion_stage_bytes_for(int s_pad, int &cb)
+{
+    const int row = s_pad * 8 + (int)sizeof(MotionRec);
+    cb = std::max(1, kFocusStageTarget / row);
+    return (int)round_up((size_t)cb * row, 128);
+}
+
+int motion_segment(const tdc_processor *p)
+{
+    if (!p->motion_fit_ok || !p->motion_enabled || !p->traj_varies || p->win_varies) return 0;
+    if (general_variant(p) != 1) return 0;  // per-sample positions only, narrow, uniform sampling
+    int cb = 1;
+    if (focus_motion_smem_bytes(motion_stage_bytes_for(p->s_pad, cb)) > 226 * 1024) return 0;  // whole rows only
+    const double rmin = min_range(p->ant_min, p->ant_max, p->grid_min, p->grid_max);
+    if (!(rmin > 0.0)) return 0;
+    const double g0 = 2.0 * std::fabs(p->F0) / kC0, g1 = 2.0 * std::fabs(p->F1) / kC0;
+    const double g_max = g0 + g1 * std::max(0, p->s_pad);
+    // psi(s) = g_s d_s: slope psi' = g1 d + g_s d', curvature c2 = psi''/2 = g1 d' + g_s d''/2, with
+    // |d| <= delta_max, |d'| <= |V1| + 2 |V2| s, |d''| <= 2 |V2| + |d'|^2 / R (1 + 10%)
+    const double dp = p->motion_v1max + 2.0 * p->motion_v2max * p->s_pad;
+    const double slope = g1 * p->delta_max + g_max * dp * 1.1;
+    const double c2 = (g1 * dp + g_max * (p->motion_v2max + dp * dp / (2.0 * rmin))) * 1.1;
+    // the segment tables rotate QL by 2 pi L slope with a series valid to 0.5 rad
+    if (!(2.0 * M_PI * 8.0 * slope <= 0.5)) return 0;
+    // longest segment whose chord (plus mean offset) stays within kMotionTolRad of psi
+    int best = 0;
+    for (int m = 8; m <= (1 << 16); m *= 2) {
+        if (2.0 * M_PI * c2 * ((double)m * m - 1.0) / 6.0 > kMotionTolRad) break;
+        best = m;
+        if (m >= p->s_pad) break;
+    }
+    return best;
+}
+
 int choose_path(const tdc_processor *p)
 {
     const int variant = general_variant(p);
@@ -626,6 +751,8 @@ int choose_path(const tdc_processor *p)
     // Per-sample range change d_s = N/(2 R0) f(N/R0^2): the series of f stays accurate for
     // |N/R0^2| <= 2 dmax/Rmin + (dmax/Rmin)^2 <= 0.1.
     if ((variant & 1) && !(range_change_bound(p) <= kGeneralMaxEps)) return TDC_PATH_GENERAL_FP64;
+    // positions moving smoothly within chirps: the per-sample phase linearised per segment
+    if (motion_segment(p) > 0) return TDC_PATH_FP32_MOTION;
     // rows of any length fit: those too long for whole-row stages are staged in segments
     return TDC_PATH_GENERAL;
 }
@@ -769,6 +896,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     // FP32 kernels read one record per chirp; the FP64 general kernel one per sample.
     const bool rec_per_sample = !p->per_chirp && path == TDC_PATH_GENERAL_FP64;
     job.chirps = p->per_chirp || rec_per_sample ? p->chirps.as<const ChirpRec>() : p->gen_rec.as<const ChirpRec>();
+    if (path == TDC_PATH_FP32_MOTION) job.chirps = reinterpret_cast<const ChirpRec *>(p->motion_rec.p);
     job.traj = p->traj_varies ? p->traj.as<const float4>() : nullptr;
     job.wins = p->win_varies ? p->wins.as<const float4>() : nullptr;
     job.wdot = p->win_varies && p->traj_varies ? p->wdot.as<const float>() : nullptr;
@@ -848,11 +976,17 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     }
     // FP32 general rows likewise: whole, or in segments of about kGeneralStageTarget bytes
     const int gen_seg = path == TDC_PATH_GENERAL ? general_seg_len(p->s_pad, variant) : 0;
-    const int stage_bytes = path == TDC_PATH_GENERAL ? general_stage_bytes_for(p->s_pad, variant, gen_seg, cb)
-                            : seg                     ? seg_stage_bytes
-                                                      : stage_bytes_for(p->s_pad, cb);
+    const int stage_bytes = path == TDC_PATH_GENERAL       ? general_stage_bytes_for(p->s_pad, variant, gen_seg, cb)
+                            : path == TDC_PATH_FP32_MOTION ? motion_stage_bytes_for(p->s_pad, cb)
+                            : seg                          ? seg_stage_bytes
+                                                           : stage_bytes_for(p->s_pad, cb);
+    const int motion_seg = path == TDC_PATH_FP32_MOTION ? motion_segment(p) : 0;
     int slots;
-    if (path == TDC_PATH_FP32_BULK) {
+    if (path == TDC_PATH_FP32_MOTION) {
+        const int bps = focus_motion_blocks_per_sm(stage_bytes);
+        if (bps <= 0) return fail(TDC_ERR_CUDA, "smooth-motion focus kernel does not fit on the device");
+        slots = p->n_sm * bps;
+    } else if (path == TDC_PATH_FP32_BULK) {
         const int bps = seg ? focus_fp32_seg_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
         slots = p->n_sm * bps;
@@ -909,7 +1043,9 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     plan.off_job = L.off_job;
     plan.off_units = L.off_units;
     plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
-    plan.job.seg_len = path == TDC_PATH_GENERAL ? gen_seg : seg ? kSegmentSamples : 0;
+    plan.job.seg_len = path == TDC_PATH_GENERAL ? gen_seg : path == TDC_PATH_FP32_MOTION ? motion_seg
+                                                          : seg                          ? kSegmentSamples
+                                                                                         : 0;
     plan.job.tile_cols = tile_cols;
     plan.job.grid_cols = p->cols;
     plan.job.n_tiles = (int)n_tiles;
@@ -1005,6 +1141,11 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
         TDC_CK(launch_focus_general(plan.variant, jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid,
                                     st),
                "focus kernel (general)");
+    } else if (path == TDC_PATH_FP32_MOTION) {
+        const int grid = std::min(n_units, slots);
+        const bool skip_zero = std::isfinite(job.half_bw) || job.tile_cols != 0;
+        TDC_CK(launch_focus_motion(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, skip_zero, st),
+               "focus kernel (smooth motion)");
     } else {
         TDC_CK(launch_focus_fp64(jobs_dev, units_dev, n_units, status, job.per_sample, st), "focus kernel (fp64)");
     }
@@ -1013,12 +1154,13 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     p->sums_epoch = store ? p->state_epoch : 0;
     p->stats.path = path;
     p->stats.correlations = (int64_t)P * C * p->S;
-    const bool staged = path == TDC_PATH_FP32_BULK || path == TDC_PATH_GENERAL;
+    const bool staged = path == TDC_PATH_FP32_BULK || path == TDC_PATH_GENERAL || path == TDC_PATH_FP32_MOTION;
     const int row = path == TDC_PATH_GENERAL ? job.seg_len : plan.seg ? kSegmentSamples : p->s_pad;
     p->stats.stage_samples = staged ? std::min(row, p->s_pad) : 0;
     p->stats.stage_chirps = staged ? (row < p->s_pad ? 1 : plan.cb) : 0;
     p->stats.general_variant = path == TDC_PATH_GENERAL ? plan.variant : 0;
     p->stats.tile_cols = job.tile_cols;
+    p->stats.motion_segment = path == TDC_PATH_FP32_MOTION ? job.seg_len : 0;
     return TDC_OK;
 }
 
@@ -1193,6 +1335,13 @@ int tdc_processor_set_skip_test(tdc_processor *p, int enable)
     if (int rc = check_proc(p)) return rc;
     p->skip_test = enable ? 1 : 0;
     p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_set_motion_path(tdc_processor *p, int enable)
+{
+    if (int rc = check_proc(p)) return rc;
+    p->motion_enabled = enable != 0;
     return TDC_OK;
 }
 

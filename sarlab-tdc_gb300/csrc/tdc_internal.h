@@ -58,6 +58,22 @@ struct __align__(16) ChirpRec {
 };
 static_assert(sizeof(ChirpRec) == 48, "ChirpRec must be 48 bytes");
 
+// One chirp's record for the smooth-motion kernel, 80 bytes (5 x float4): positions of
+// the chirp's samples as P[c, s] = P0 + V1 s + V2 s^2 (the host's fit of the per-sample
+// positions).
+//   p_hi.xyz, p_lo.xyz  P0 as double-float pairs; p_hi.w = Doppler window centre [Hz]; p_lo.w = 0
+//   vel.xyz             velocity at sample 0 (Doppler window); vel.w = 2 V1.V2
+//   v1.xyz              V1 [m / sample]; v1.w = |V1|^2
+//   v2.xyz              V2 [m / sample^2]; v2.w = |V2|^2
+struct __align__(16) MotionRec {
+    float4 p_hi;
+    float4 p_lo;
+    float4 vel;
+    float4 v1;
+    float4 v2;
+};
+static_assert(sizeof(MotionRec) == 80, "MotionRec must be 80 bytes");
+
 // One sample point of the reference's chunk skip test (tdcprocessor.cpp:355-378).
 struct __align__(16) SkipPoint {
     float4 pos_fdc;  // position xyz, window centre
@@ -165,6 +181,13 @@ int focus_fp32_seg_blocks_per_sm(int stage_bytes);
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,
                               bool skip_zero, bool store_sums, cudaStream_t st);
+// Smooth-motion focus (tdc_motion.cu): per-sample positions given by job.chirps as
+// MotionRec records, rows staged whole (stage_bytes >= chirps x (s_pad x 8 + 80)),
+// psi linearised over segments of job.seg_len samples (a power of two >= 8).
+cudaError_t launch_focus_motion(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
+                                int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero, cudaStream_t st);
+int focus_motion_blocks_per_sm(int stage_bytes);
+int focus_motion_smem_bytes(int stage_bytes);
 // Plain FP64-phase focus (comparator and general fallback), one CTA per unit.
 cudaError_t launch_focus_fp64(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *status_dev, int per_sample, cudaStream_t st);

@@ -155,6 +155,13 @@ struct tdc_processor {
     bool sample_recs_ready = false;  // chirps holds the per-(chirp, sample) records
     bool win_varies = false;    // the Doppler window can differ within a chirp (finite band, per-sample motion)
     double delta_max = 0.0;     // max |P[c,s] - P[c,0]| [m]
+    // Smooth intra-chirp motion: every chirp's per-sample positions are P0 + V1 s + V2 s^2 to
+    // within the rounding of their FP32 values (motion_rec holds the fits); the smooth-motion
+    // kernel then runs instead of the FP32 general kernel, unless switched off.
+    bool motion_fit_ok = false;
+    bool motion_enabled = true;
+    double motion_v1max = 0.0;  // max |V1| [m / sample]
+    double motion_v2max = 0.0;  // max |V2| [m / sample^2]
     double F0 = 0.0, F1 = 0.0, resid_hz = 0.0;
     double ant_min[3] = {0, 0, 0}, ant_max[3] = {0, 0, 0};
     int s_pad = 0, n_chunks = 0;
@@ -162,6 +169,8 @@ struct tdc_processor {
     // FP32 general path: sample-0 records per chirp (when chirps holds one per sample),
     // per-sample offsets / windows, residual frequency table.
     tdc::impl::DevBuf gen_rec, traj, wins, wdot, gres;
+    // Smooth-motion kernel: one MotionRec per chirp.
+    tdc::impl::DevBuf motion_rec;
     // Autofocus: the forward's per-(chirp, pixel) sums and the rows pre-scaled by the sample
     // index, so the adjoint computes only the index-weighted sums (keep_sums on).
     tdc::impl::DevBuf chirp_sums, xs_scaled;
@@ -204,7 +213,7 @@ struct tdc_processor {
     {
         return {&xw,      &chirps,     &skip,    &gs,      &pos_base, &wr,      &offsets,     &flag,     &gen_rec,
                 &traj,    &wins,       &wdot,    &gres,    &grid_stage, &grid_hi, &grid_lo, &scratch, &adj_scratch,
-                &chirp_sums, &xs_scaled,
+                &chirp_sums, &xs_scaled, &motion_rec,
                 &image_dev};
     }
 };
@@ -244,6 +253,10 @@ int general_segment_samples(int s_pad, int variant);
 int general_seg_len(int s_pad, int variant);
 // Variant bits of the FP32 general kernel for the resident acquisition.
 int general_variant(const tdc_processor *p);
+// Segment length (samples, a power of two) of the smooth-motion kernel for the resident
+// acquisition and grid, or 0 when that kernel does not take them.
+int motion_segment(const tdc_processor *p);
+int motion_stage_bytes_for(int s_pad, int &cb);
 FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path);
 // Plan units (p->units_host) and make sure the processor's scratch holds them and the partials.
 // max_unit_work > 0 bounds the correlations of one unit (the request loop's granularity).

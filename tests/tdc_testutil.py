@@ -39,7 +39,7 @@ def problem_from_api(api: dict, grid, pos64=None, grid64=False) -> oracle.Proble
                           startFreq=api["startFreq"], grid=g, bodyBoresight=tuple(api["bodyBoresight"]))
 
 
-def run_engine(api: dict, grid, start_args, pos64=None, grid64=None, precision="fp32", skip_test=True):
+def run_engine(api: dict, grid, start_args, pos64=None, grid64=None, precision="fp32", skip_test=True, motion=True):
     import _sarlabtdc
 
     p = _sarlabtdc.TdcProcessor(0)
@@ -53,5 +53,6 @@ def run_engine(api: dict, grid, start_args, pos64=None, grid64=None, precision="
         p.setFocusGrid(grid)
     p.setPrecision(precision)
     p.setSkipTest(skip_test)
+    p.setMotionPath(motion)
     p.start(*start_args)
     return p.getFocusedImage(), p.lastStats(), p

@@ -380,7 +380,7 @@ def test_fp32_general_kernel_variants(cuda_device, case):
     nonunif = "nonunif" in case or case == "all"
     api = _general_api(sc, traj=traj, win=win, nonunif=nonunif, drift=3e-3 if case == "traj_wide" else 0.3e-3)
     args = (0.0, 30.0 if win else INF, False, True, True)
-    img, stats, _ = run_engine(api, sc.grid, args)
+    img, stats, _ = run_engine(api, sc.grid, args, motion=False)
     assert stats["path_name"] == "general"
     ref = _oracle(api, sc.grid, args).reshape(img.shape)
     if win:
@@ -499,7 +499,7 @@ def test_fp32_general_kernel_long_chirps_in_segments(cuda_device, case, n_sample
     nonunif = "nonunif" in case or case == "all"
     api = _general_api(sc, traj=traj, win=win, nonunif=nonunif, drift=0.1e-3)
     args = (0.0, 30.0 if win else INF, False, True, True)
-    img, stats, _ = run_engine(api, sc.grid, args)
+    img, stats, _ = run_engine(api, sc.grid, args, motion=False)
     assert stats["path_name"] == "general"
     assert 0 < stats["stage_samples"] < n_samples and stats["stage_chirps"] == 1
     assert stats["stage_samples"] % 16 == 0
@@ -514,7 +514,7 @@ def test_fp32_general_kernel_stages_whole_rows_when_they_fit(cuda_device):
     """Short per-sample rows are staged whole, several chirps a stage."""
     sc = scenes.small_scene(seed=92, n_pri=64, n_samples=64, nx=8, ny=8, device="cuda")
     api = _general_api(sc, traj=True)
-    img, stats, _ = run_engine(api, sc.grid, (0.0, INF, False, True, True))
+    img, stats, _ = run_engine(api, sc.grid, (0.0, INF, False, True, True), motion=False)
     assert stats["path_name"] == "general"
     assert stats["stage_samples"] == 64 and stats["stage_chirps"] > 1
     _check(img, _oracle(api, sc.grid, (0.0, INF, False, True, True)).reshape(img.shape))
@@ -526,20 +526,23 @@ def test_parity_ragged_shapes(cuda_device, n_pri, n_samples, nx, ny):
     """Ragged acquisitions: one chirp, one sample, one pixel, chirp counts either side of
     the 128-chirp skip chunk, pixel counts either side of the 512-pixel tile; an unbounded
     band and a finite one (per-chirp windows, skip test on partial chunks) on the FP32-bulk
-    kernel, and positions moving within the chirps on the FP32 general kernel."""
+    kernel, and positions moving within the chirps on the smooth-motion kernel and on the
+    FP32 general kernel."""
     sc = scenes.small_scene(seed=100 + n_pri + n_samples, n_pri=n_pri, n_samples=n_samples, nx=nx, ny=ny,
                             device="cuda")
-    cases = [(_scene_api(sc), (0.0, INF, False, True, True), "fp32_bulk"),
-             (_moving_api(sc, speed=0.08), (2.0, 18.0, False, True, True), "fp32_bulk")]
+    cases = [(_scene_api(sc), (0.0, INF, False, True, True), "fp32_bulk", True),
+             (_moving_api(sc, speed=0.08), (2.0, 18.0, False, True, True), "fp32_bulk", True)]
     if n_samples > 1:
-        cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "general"))
+        cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "general", False))
+    if n_samples > 2:
+        cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "fp32_motion", True))
     rng = np.random.default_rng(n_pri + n_samples)
-    for api, args, path in cases:
+    for api, args, path, motion in cases:
         if not np.any(api["rawData"]):
             # a one-sample chirp simulated under a Hann taper is all zero: use seeded noise
             raw = rng.normal(size=(n_pri, n_samples, 2)).astype(np.float32)
             api["rawData"] = np.ascontiguousarray(raw[..., 0] + 1j * raw[..., 1]).astype(np.complex64)
-        img, stats, _ = run_engine(api, sc.grid, args)
+        img, stats, _ = run_engine(api, sc.grid, args, motion=motion)
         assert img.shape == (ny, nx)
         assert stats["path_name"] == path
         ref = _oracle(api, sc.grid, args).reshape(img.shape)

@@ -220,7 +220,7 @@ def test_noalloc_finite_band_and_skip_points_against_the_oracle(cuda_device, tap
     sc = scenes.small_scene(seed=64, n_pri=750, n_samples=64, nx=21, ny=17, rail_len=0.75, device="cuda")
     api = sc.api_arrays()
     vel = np.zeros_like(api["velocity"])
-    vel[..., 0] = 0.05
+    vel[..., 0] = 0.2
     api["velocity"] = vel
     centre, band = 2.0, 18.0
     a, keep = _noalloc_args(api, sc.grid, torch, centre=centre, band=band, taper=taper, skip=True)
@@ -232,7 +232,7 @@ def test_noalloc_finite_band_and_skip_points_against_the_oracle(cuda_device, tap
     assert rel_l2(ref, full) > 0.05                      # the window does cut pixels' chirps
     no_skip = oracle.focus(prob, oracle.Opts(dopplerWinCenter=centre, dopplerBandwidth=band, applyRangeWin=False,
                                              dopplerWinTaper=taper, skip_test=False))
-    assert np.any(ref != no_skip)                        # and the skip test drops whole chunks
+    assert rel_l2(ref, no_skip) > 0.05                   # and the skip test drops whole chunks
     # chirps at the inclusive band edge may fall either side in FP32: L2 bound only
     assert rel_l2(got, ref) <= 2e-4
 
