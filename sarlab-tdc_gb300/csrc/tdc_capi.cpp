@@ -389,9 +389,9 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
 
     // ---- smooth intra-chirp motion (the smooth-motion kernel) ----
     // Least-squares fit of each chirp's D_s = P[c,s] - P[c,0] by V0 + V1 s + V2 s^2 (orthogonal
-    // polynomials in the centred index); accepted when every sample's residual stays within one
+    // polynomials in the centred index); accepted when every sample's residual stays within two
     // ulp of the chirp's largest FP32 coordinate on that axis, i.e. what remains is the rounding
-    // of the input.
+    // of the input (up to half an ulp per sample, spread a little further by the fit).
     std::vector<MotionRec> mrecs;
     p->motion_fit_ok = false;
     p->motion_v1max = p->motion_v2max = 0.0;
@@ -435,7 +435,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
                     for (int s = 0; s < S && !fail_fit; ++s) {
                         const double y = (double)p->pos[3 * ti(c, s) + k] - (double)p0[k];
                         const double r = y - (V0[k] + s * (V1[k] + s * V2[k]));
-                        if (!(std::fabs(r) <= ulp)) fail_fit = true;
+                        if (!(std::fabs(r) <= 2.0 * ulp)) fail_fit = true;
                     }
                 }
                 if (fail_fit) break;
@@ -709,6 +709,15 @@ int motion_stage_bytes_for(int s_pad, int &cb)
     return (int)round_up((size_t)cb * row, 128);
 }
 
+// Upper bound on |psi'| [cycles / sample] of the smooth-motion kernel (see motion_segment).
+double motion_slope_bound(const tdc_processor *p)
+{
+    const double g0 = 2.0 * std::fabs(p->F0) / kC0, g1 = 2.0 * std::fabs(p->F1) / kC0;
+    const double g_max = g0 + g1 * std::max(0, p->s_pad);
+    const double dp = p->motion_v1max + 2.0 * p->motion_v2max * p->s_pad;
+    return g1 * p->delta_max + g_max * dp * 1.1;
+}
+
 int motion_segment(const tdc_processor *p)
 {
     if (!p->motion_fit_ok || !p->motion_enabled || !p->traj_varies || p->win_varies) return 0;
@@ -722,10 +731,9 @@ int motion_segment(const tdc_processor *p)
     // psi(s) = g_s d_s: slope psi' = g1 d + g_s d', curvature c2 = psi''/2 = g1 d' + g_s d''/2, with
     // |d| <= delta_max, |d'| <= |V1| + 2 |V2| s, |d''| <= 2 |V2| + |d'|^2 / R (1 + 10%)
     const double dp = p->motion_v1max + 2.0 * p->motion_v2max * p->s_pad;
-    const double slope = g1 * p->delta_max + g_max * dp * 1.1;
+    const double slope = motion_slope_bound(p);
     const double c2 = (g1 * dp + g_max * (p->motion_v2max + dp * dp / (2.0 * rmin))) * 1.1;
-    // the segment tables rotate QL by 2 pi L slope with a series valid to 0.5 rad
-    if (!(2.0 * M_PI * 8.0 * slope <= 0.5)) return 0;
+    if (!std::isfinite(slope)) return 0;
     // longest segment whose chord (plus mean offset) stays within kMotionTolRad of psi
     int best = 0;
     for (int m = 8; m <= (1 << 16); m *= 2) {
@@ -981,6 +989,9 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
                             : seg                          ? seg_stage_bytes
                                                            : stage_bytes_for(p->s_pad, cb);
     const int motion_seg = path == TDC_PATH_FP32_MOTION ? motion_segment(p) : 0;
+    // the segment's block step QL_m = QL e^{j 2 pi L sigma_m}: a rotation series for L |sigma| up
+    // to 0.8 rad, else an accurate sincos per segment
+    const bool motion_exact_ql = path == TDC_PATH_FP32_MOTION && !(2.0 * M_PI * 8.0 * motion_slope_bound(p) <= 0.8);
     int slots;
     if (path == TDC_PATH_FP32_MOTION) {
         const int bps = focus_motion_blocks_per_sm(stage_bytes);
@@ -1046,6 +1057,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     plan.job.seg_len = path == TDC_PATH_GENERAL ? gen_seg : path == TDC_PATH_FP32_MOTION ? motion_seg
                                                           : seg                          ? kSegmentSamples
                                                                                          : 0;
+    if (motion_exact_ql) plan.job.flags |= kFlagMotionExactQL;
     plan.job.tile_cols = tile_cols;
     plan.job.grid_cols = p->cols;
     plan.job.n_tiles = (int)n_tiles;

@@ -84,6 +84,7 @@ static_assert(sizeof(SkipPoint) == 32, "SkipPoint must be 32 bytes");
 enum FocusFlags : int {
     kFlagTaper = 1,     // dopplerWinTaper
     kFlagSkipTest = 2,  // apply the per-chunk skip test
+    kFlagMotionExactQL = 4,  // smooth-motion kernel: block step per segment from an accurate sincos
 };
 
 // Everything a focus kernel needs about one job (acquisition x grid).

@@ -71,7 +71,7 @@ __device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2
     return make_float2(tr, ti);
 }
 
-// (cos t, sin t) for |t| <= 0.5 by their Taylor series to t^8 / t^9 (error < 1e-9).
+// (cos t, sin t) for |t| <= 0.8 by their Taylor series to t^8 / t^9 (error < 3e-8).
 __device__ __forceinline__ float2 sincos_small(float t)
 {
     const float t2 = t * t;
@@ -176,6 +176,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_MOTION_MINB)
         const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
         const bool taper = (sJ.flags & kFlagTaper) != 0;
         const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
+        const bool exact_ql = (sJ.flags & kFlagMotionExactQL) != 0;
         const int chunk = sJ.chunk;
         const SkipPoint *__restrict__ skip = sJ.skip;
         // segments: M samples (a power of two >= kL), the last one s_pad - (nseg - 1) M
@@ -311,7 +312,16 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_MOTION_MINB)
                         p[i][0] = make_float2(c1s, s1);
 #pragma unroll
                         for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
-                        ql[i] = cmul(qlb[i], sincos_small(kTwoPiF * (float)kL * sg));
+                        if (exact_ql) {
+                            // L (beta + sigma) = frac(L bh) + L (bl + sigma) cycles: exact terms
+                            const float lbh = (float)kL * bh[i];
+                            const float lfr = (lbh - rintf(lbh)) + (float)kL * (bl[i] + sg);
+                            float sl, cl;
+                            sincospif(2.0f * lfr, &sl, &cl);
+                            ql[i] = make_float2(cl, sl);
+                        } else {
+                            ql[i] = cmul(qlb[i], sincos_small(kTwoPiF * (float)kL * sg));
+                        }
                         if (m == nseg - 2) {
                             // entering the first full segment after the (shorter) last one
                             const float2 r = make_float2(fmaf(-0.5f * dq[i], dq[i], 1.0f), dq[i]);

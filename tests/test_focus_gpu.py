@@ -535,7 +535,10 @@ def test_parity_ragged_shapes(cuda_device, n_pri, n_samples, nx, ny):
     if n_samples > 1:
         cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "general", False))
     if n_samples > 2:
-        cases.append((_general_api(sc, traj=True), (0.0, INF, False, True, True), "fp32_motion", True))
+        # motion of a micrometre within the chirp: short rows with more motion change the phase
+        # too fast along the chirp for the smooth-motion kernel's segments (the general kernel
+        # takes them, as above)
+        cases.append((_general_api(sc, traj=True, drift=1e-6), (0.0, INF, False, True, True), "fp32_motion", True))
     rng = np.random.default_rng(n_pri + n_samples)
     for api, args, path, motion in cases:
         if not np.any(api["rawData"]):
