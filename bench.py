@@ -837,11 +837,128 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sharded(args):
+    """N GPUs, one process each (torchrun): pixel sharding with weak scaling. Every rank holds
+    the whole precision-study acquisition and focuses its own 1024-row block of a grid of
+    N x 1024 rows (the scene's grid shifted by its block along y), planned for the whole grid
+    (setPlanPixels). No data moves between ranks while they focus; `value` = all ranks'
+    correlations / the slowest rank's time. `e2e`: the sharded processor with host buffers
+    (setRawData, setFocusGrid, start, the image gathered on every rank)."""
+    import torch
+    import torch.distributed as dist
+
+    import _sarlabtdc
+    from sarlabtdc import sharding
+
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    sc = make_scene(args, "cuda")
+    api = sc.api_arrays()
+    rows, cols = sc.grid.shape[:2]
+    grid = sc.grid.copy()
+    grid[..., 1] += rank * rows * 1e-3
+    corr = sc.correlations()
+    start_args = (0.0, float("inf"), False, False, True)
+    p = _sarlabtdc.TdcProcessor(local)
+    p.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                 api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+    p.setChirpPositionsF64(sc.positions)
+    p.setFocusGridF64(grid)
+    p.setPlanPixels(world * rows * cols)
+    p.prepare(*start_args)
+    p.uploadGrid()
+    img = torch.empty(sc.n_pix, dtype=torch.complex64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        p.focusDevice(img, stream)
+        flush.zero_()
+    p.check(stream)
+    clocks = Clocks()
+    if rank == 0:
+        clocks.start()
+        time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e0, e1 in evs:
+        e0.record(stream)
+        p.focusDevice(img, stream)
+        e1.record(stream)
+        flush.zero_()
+    torch.cuda.synchronize()
+    wall = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+    dist.barrier()
+    clk = clocks.stop() if rank == 0 else None
+    p.check(stream)
+    kernel_ms = torch.tensor([float(np.mean([a.elapsed_time(b) for a, b in evs]))], dtype=torch.float64,
+                             device="cuda")
+    dist.all_reduce(wall, op=dist.ReduceOp.MAX)
+    dist.all_reduce(kernel_ms, op=dist.ReduceOp.MAX)
+    total_s = float(wall.item())
+    value = world * corr * args.steps / total_s / 1e9
+
+    # e2e: host buffers through the sharded processor, image gathered on every rank
+    tall = np.concatenate([sc.grid + np.array([0.0, r * rows * 1e-3, 0.0]) for r in range(world)], axis=0)
+    sp = sharding.ShardedProcessor(local, rank, world)
+    times = []
+    for i in range(3):
+        dist.barrier()
+        t = time.perf_counter()
+        sp.setRawData(api["rawData"], api["priTimes"], api["sampleTimes"], api["position"], api["velocity"],
+                      api["attitude"], api["modRate"], api["startFreq"], api["bodyBoresight"])
+        sp.setChirpPositionsF64(sc.positions)
+        sp.setFocusGridF64(tall)
+        sp.start(*start_args)
+        full = sp.getFocusedImage()
+        dt = torch.tensor([time.perf_counter() - t], dtype=torch.float64, device="cuda")
+        dist.all_reduce(dt, op=dist.ReduceOp.MAX)
+        if i > 0:
+            times.append(float(dt.item()))
+    stats = sp.proc.lastStats()
+    if rank == 0:
+        peak_tf, fp64_tf, _ = fp32_peak_tflops(_tdc_lib(), torch)
+        achieved = corr / (float(kernel_ms.item()) / 1e3) / 1e9 * FLOP_PER_CORR / 1e3
+        out = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": round(1e3 * total_s / args.steps, 3), "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded point targets + complex Gaussian noise, FP64 jittered trajectory)",
+               "config": bench_config(args, sc),
+               "run": {"correlations_per_step": world * corr, "sharding": f"{world} row blocks of {rows} x {cols} "
+                       "pixels, one per GPU, the whole acquisition on every GPU, no collective while focusing",
+                       "path": p.path()},
+               "gpu_launches": 2 * args.steps, "clocks": clk,
+               "roofline": {"bound": "fp32", "achieved": round(achieved, 2), "peak": round(peak_tf, 2),
+                            "unit": "TFLOP/s", "frac": round(achieved / peak_tf, 4), "traffic": None,
+                            "peak_source": "measured FFMA probe (tdc_probe_fma) on rank 0's GPU, this run",
+                            "kernel": "focus_fp32_kernel (slowest rank)"},
+               "e2e": {"value": round(world * corr / float(np.mean(times)) / 1e9, 2), "unit": UNIT,
+                       "h2d_bytes_per_step": int(stats["h2d_bytes"]) * world,
+                       "d2h_bytes_per_step": int(stats["d2h_bytes"]) * world, "steps": len(times),
+                       "gathered_image_bytes": int(full.nbytes)}}
+        print(json.dumps(out), flush=True)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def _tdc_lib():
+    import _tdc_capi
+
+    return _tdc_capi.lib()
+
+
 def main():
     args = parse()
-    if args.gpus != 1 and args.impl == "ours":
-        print(json.dumps({"error": "this engine runs one process on one GPU; run with --gpus 1"}))
-        return 2
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "ours" and (args.gpus > 1 or world > 1):
+        if world != args.gpus or args.config != "2":
+            print(json.dumps({"error": "--gpus N runs the precision study under torchrun with N processes"}))
+            return 2
+        run_sharded(args)
+        return 0
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "4":

@@ -171,6 +171,14 @@ int tdc_range_window(float *w_dev, int n_samples, int apply_range_win, void *str
  * at the next start() / prepare(). */
 int tdc_processor_set_skip_test(tdc_processor *proc, int enable);
 
+/* Plan the chirp groups of the next focuses as for a grid of n_pix pixels (0, default: the
+ * resident grid's own count). A pixel's summation order depends only on the chirp groups, so
+ * a processor focusing a block of rows of a larger grid gives, with the larger grid's pixel
+ * count set here, bit for bit the values a focus of the whole grid gives on the same kind of
+ * GPU (pixel sharding across GPUs, sarlabtdc.sharding). Extension without a reference
+ * counterpart (the reference binds one GPU, tdcprocessor.cpp:39-55). */
+int tdc_processor_set_plan_pixels(tdc_processor *proc, int64_t n_pix);
+
 /* Smooth-motion path (TDC_PATH_FP32_MOTION) on (1, default) or off (0: such inputs take
  * the FP32 general kernel). Extension without a reference counterpart; takes effect at the
  * next focus. */

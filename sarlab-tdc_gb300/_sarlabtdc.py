@@ -206,6 +206,11 @@ class TdcProcessor:
         code = {"fp32": _lib.PRECISION_FP32_BULK, "fp64": _lib.PRECISION_FP64_PHASE}[precision]
         _lib.check(_lib.lib().tdc_processor_set_precision(self._h, code))
 
+    def setPlanPixels(self, n_pix: int):
+        """Extension: plan the chirp groups as for a grid of n_pix pixels (0: the grid's own), so
+        a row block of a larger grid focuses bit for bit like that grid (pixel sharding)."""
+        _lib.check(_lib.lib().tdc_processor_set_plan_pixels(self._h, int(n_pix)))
+
     def setMotionPath(self, enable: bool):
         """Extension: per-sample positions that move smoothly within each chirp take the
         smooth-motion kernel (default) or, when off, the FP32 general kernel."""

@@ -157,6 +157,7 @@ SIGNATURES = [
     ("tdc_range_window", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     ("tdc_processor_set_skip_test", C.c_int, [_vp, C.c_int]),
     ("tdc_processor_set_motion_path", C.c_int, [_vp, C.c_int]),
+    ("tdc_processor_set_plan_pixels", C.c_int, [_vp, C.c_int64]),
     ("tdc_processor_prepare", C.c_int, [_vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]),
     ("tdc_processor_upload_grid", C.c_int, [_vp]),
     ("tdc_processor_focus_device", C.c_int, [_vp, _vp, _vp]),

@@ -1013,10 +1013,15 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     const long long n_tiles = tile_count(P, tile_cols, p->cols);
     // (block tiles also depend on the grid's shape, not only on its pixel count)
     const int plan_cols = tile_cols ? p->cols : 0;
+    // The chirp groups (each pixel's summation order) follow the grid the job is planned for:
+    // its own, or a larger one whose row block this grid is (pixel sharding across GPUs).
+    const long long plan_tiles = p->plan_pixels > P ? tile_count(p->plan_pixels, tile_cols, p->cols) : n_tiles;
     if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
-        max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols || plan_cols != p->plan_cols) {
-        plan_groups(n_tiles, C, slots, p->plan_groups, p->plan_cpg,
+        max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols || plan_cols != p->plan_cols ||
+        plan_tiles != p->plan_tiles) {
+        plan_groups(plan_tiles, C, slots, p->plan_groups, p->plan_cpg,
                     path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot);
+        p->plan_tiles = plan_tiles;
         if (max_unit_work > 0) {
             // bound the work of one unit (tile x chirp group): at most cap / (tile x S) chirps per group
             const int cpg_cap = std::max(1, (int)(max_unit_work / ((double)kFocusTile * p->S)));
@@ -1347,6 +1352,14 @@ int tdc_processor_set_skip_test(tdc_processor *p, int enable)
     if (int rc = check_proc(p)) return rc;
     p->skip_test = enable ? 1 : 0;
     p->prepared = false;
+    return TDC_OK;
+}
+
+int tdc_processor_set_plan_pixels(tdc_processor *p, int64_t n_pix)
+{
+    if (int rc = check_proc(p)) return rc;
+    if (n_pix < 0) return fail(TDC_ERR_INVALID_ARGUMENT, "n_pix must not be negative");
+    p->plan_pixels = n_pix;
     return TDC_OK;
 }
 

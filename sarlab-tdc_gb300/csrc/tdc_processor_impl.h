@@ -194,6 +194,8 @@ struct tdc_processor {
     int plan_C = -1, plan_groups = 0, plan_cpg = 0, plan_path = -1, plan_slots = 0, plan_tile_cols = -1,
         plan_cols = -1;
     double plan_unit_cap = 0.0;
+    long long plan_tiles = -1;   // tiles the chirp groups were planned for
+    long long plan_pixels = 0;   // plan the chirp groups for a grid of this many pixels (0: the grid's own)
     bool plan_uploaded = false;
 
     // Adjoint (autofocus) scratch.

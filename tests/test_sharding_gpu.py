@@ -1,0 +1,51 @@
+"""Pixel sharding on the GPU: the row blocks of a grid, focused one after another on this
+GPU as the ranks of a sharded focus would focus them (blocks are independent: no rank waits
+for another), assemble into the whole grid's image bit for bit when each block plans its
+chirp groups for the whole grid (ShardedProcessor does), and agree with it to FP32 rounding
+when each plans for itself."""
+import numpy as np
+import pytest
+
+from sarlabtdc import scenes, sharding
+from tdc_testutil import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+START = (0.0, float("inf"), False, True, True)
+
+
+class _NoGroupSharded(sharding.ShardedProcessor):
+    """A rank's processor without a process group: the blocks are assembled by the test."""
+
+
+def _focus_blocks(sc, api, world, pin):
+    import _sarlabtdc
+
+    out = np.empty(sc.grid.shape[:2], np.complex64)
+    for rank in range(world):
+        sp = _NoGroupSharded(0, rank, world)
+        sp.setRawData(*api.values())
+        sp.setFocusGrid(sc.grid.astype(np.float32))
+        if not pin:
+            sp.proc.setPlanPixels(0)
+        sp.start(*START)
+        r0, r1 = sp.rows
+        out[r0:r1] = sp.getLocalImage()
+        assert isinstance(sp.proc, _sarlabtdc.TdcProcessor)
+    return out
+
+
+@pytest.mark.parametrize("world", [2, 3, 5])
+def test_blocks_assemble_the_whole_grid_bit_for_bit(cuda_device, world):
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=301, n_pri=1024, n_samples=128, nx=128, ny=257, jitter=0.2e-3, device="cuda")
+    api = sc.api_arrays()
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setFocusGrid(sc.grid.astype(np.float32))
+    p.start(*START)
+    whole = p.getFocusedImage()
+    np.testing.assert_array_equal(_focus_blocks(sc, api, world, pin=True), whole)
+    # planned per block, the chirp groups (each pixel's summation order) may differ: FP32 rounding
+    assert rel_l2(_focus_blocks(sc, api, world, pin=False), whole) < 1e-6
