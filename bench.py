@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the oracle accuracy check")
     ap.add_argument("--general-only", action="store_true",
                     help="config 2 scene: only the FP32 vs FP64 general-kernel leg (per-sample trajectory)")
+    ap.add_argument("--windowed-only", action="store_true",
+                    help="config 2 scene: only the windowed leg (moving antenna, finite Doppler band)")
     return ap.parse_args()
 
 
@@ -664,6 +666,26 @@ def serving_leg(args):
             "clocks": clk}
 
 
+def run_windowed_only(args):
+    """The windowed leg of the precision-study scene on its own (a JSON line): the whole grid
+    with the antenna moving along the rail under a 10 Hz Doppler band."""
+    import torch
+
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    torch.cuda.set_device(0)
+    sc = make_scene(args, "cuda")
+    build_oracle()
+    res = run_windowed(sc, sc.api_arrays(), True, torch.cuda.current_stream(), float("nan"))
+    res.pop("unbounded_ms", None)
+    res.pop("speedup_vs_unbounded", None)
+    out = {"metric": "windowed focus: ms per focus", "unit": "ms", "value": res["ms"], "higher_is_better": False,
+           "dtype": "f32", "n_gpus": 1,
+           "config": {"workload": f"{args.side}x{args.side} px precision-study grid, {sc.n_pri} chirps x "
+                                  f"{sc.n_samples} samples, antenna at 0.05 m/s along the rail, 10 Hz band"},
+           "windowed": res}
+    print(json.dumps(out), flush=True)
+
+
 def run_serving(args):
     """Config 4 alone: one JSON line."""
     sv = serving_leg(args)
@@ -967,6 +989,8 @@ def main():
         run_autofocus(args)
     elif args.general_only:
         run_general_only(args)
+    elif args.windowed_only:
+        run_windowed_only(args)
     else:
         run_ours(args)
     return 0
