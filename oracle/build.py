@@ -107,11 +107,41 @@ def build_ref_ptx(force: bool = False) -> Path | None:
     return REF_PTX
 
 
+REF_HOST_LOOP = REF_OUT / "ref_host_loop"
+HOST_LOOP_SRC = HERE.parent / "tests" / "golden" / "ref_host_loop.cpp"
+
+
+def build_ref_host_loop(force: bool = False) -> Path | None:
+    """The timing harness of the reference's GPU path (tests/golden/ref_host_loop.cpp: its host
+    loop restated, its kernels from REF_PTX, NPP's sum) for this machine, or None where the CUDA
+    toolkit's NPP headers or libraries are missing. Built from our own source, on any machine."""
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    if not (cuda / "include" / "npps.h").is_file():
+        return None
+    if not force and not _stale(REF_HOST_LOOP, [HOST_LOOP_SRC, Path(__file__)]):
+        return REF_HOST_LOOP
+    REF_OUT.mkdir(exist_ok=True)
+    tmp = REF_HOST_LOOP.with_suffix(".tmp%d" % os.getpid())
+    libdirs = [cuda / "lib64", cuda / "lib64" / "stubs", cuda / "targets" / "sbsa-linux" / "lib",
+               cuda / "targets" / "sbsa-linux" / "lib" / "stubs"]
+    cmd = ["g++", "-O2", "-std=c++17", "-I", str(cuda / "include"), str(HOST_LOOP_SRC), "-o", str(tmp)]
+    for d in libdirs:
+        if d.is_dir():
+            cmd += ["-L", str(d)]
+    cmd += ["-lnpps", "-lnppc", "-lcudart", "-lcuda"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    os.replace(tmp, REF_HOST_LOOP)
+    return REF_HOST_LOOP
+
+
 def main(argv: list[str]) -> int:
     force = "--force" in argv
     print(build_oracle(force))
     print(build_refmath(force))
     print(build_ref_ptx(force))
+    print(build_ref_host_loop(force))
     return 0
 
 

@@ -314,6 +314,14 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         for (int c = cb; c < ce; ++c) recs[c] = make_record(p, c, 0, o.centroid != 0, o.center);
     });
     p->sample_recs_ready = false;
+    // With an unbounded band the window is 1 wherever the range is positive, provided the
+    // velocities and window centres are finite (else the reference's window is NaN -> 0).
+    p->unit_window_ok = true;
+    for (int c = 0; c < C && p->unit_window_ok; ++c) {
+        const ChirpRec &r = recs[c];
+        p->unit_window_ok = std::isfinite(r.vel.x) && std::isfinite(r.vel.y) && std::isfinite(r.vel.z) &&
+                            std::isfinite(r.p_hi.w);
+    }
     {
         double v[3] = {0.0, 0.0, 0.0};
         for (int c = 0; c < C; ++c) {
@@ -924,6 +932,7 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     job.chunk = kChunk;
     job.stage_chirps = cb;
     job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
+    if (std::isinf(p->opts.bw) && p->opts.bw > 0.f && p->unit_window_ok) job.flags |= kFlagUnitWindow;
     job.n_tiles = (int)((p->P + kFocusTile - 1) / kFocusTile);
     job.per_sample = rec_per_sample ? 1 : 0;
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;

@@ -158,6 +158,7 @@ struct tdc_processor {
     // Smooth intra-chirp motion: every chirp's per-sample positions are P0 + V1 s + V2 s^2 to
     // within the rounding of their FP32 values (motion_rec holds the fits); the smooth-motion
     // kernel then runs instead of the FP32 general kernel, unless switched off.
+    bool unit_window_ok = false;  // every chirp record's velocity and window centre are finite
     bool motion_fit_ok = false;
     bool motion_enabled = true;
     double motion_v1max = 0.0;  // max |V1| [m / sample]

@@ -1,14 +1,19 @@
 """Time the reference's own GPU kernels on a pixel sample of a focus workload and compare
 the engine's image with theirs.
 
-Like make_ref_gpu_golden.py (whose loader and launch sequence it reuses), this runs on a
-machine with a GPU and oracle/_ref/tdckernels.ptx (built by oracle/build.py from the
-reference's tdc-lib/src/tdckernels.cu). The reference's host loop
-(tdc-lib/src/tdcprocessor.cpp:59-167) needs spdlog and NPP, so it is emulated from Python
-in the same order -- per chunk of 128 PRIs and per pixel: window, reference response and
-correlation kernels, then a device sum added to the pixel on the device -- which is, if
-anything, lighter than the reference's per-call NPP context set-up. The pixel sample's
-time gives the reference path's per-pixel cost; Gcorr/s = chirps x samples / that cost.
+Runs on a machine with a GPU and oracle/_ref/tdckernels.ptx (built by oracle/build.py from
+the reference's tdc-lib/src/tdckernels.cu). Two timings of the same launch sequence:
+
+* ``host_loop``: oracle/_ref/ref_host_loop (tests/golden/ref_host_loop.cpp, built by
+  oracle/build.py on the GPU machine) -- the host loop of tdc-lib/src/tdcprocessor.cpp:
+  59-167 restated in C++ around the reference's kernels, with NPP's nppsSum_32fc_Ctx and
+  its NppStreamContext filled per call as tdc-lib/src/npp_utils.cpp:9-27 does, and
+  addToImage<<<1, 1>>>: the reference's GPU path as its own host code drives it;
+* ``python_loop``: the same kernels launched from Python (make_ref_gpu_golden.py's loader),
+  the chunk sum taken on the device by torch instead of NPP.
+
+The pixel sample's time gives the path's per-pixel cost; Gcorr/s = chirps x samples / that
+cost.
 
     python tests/golden/time_ref_gpu_kernels.py [workload] [n_pixels]
 
@@ -29,6 +34,48 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 
 import make_ref_gpu_golden as ref  # noqa: E402
+
+
+def run_host_loop(case, ptx: Path, repeats: int = 2):
+    """(timing JSON, image) of oracle/_ref/ref_host_loop on the case (best of `repeats` runs),
+    or None where it cannot be built."""
+    import subprocess
+    import tempfile
+
+    from oracle import build as ob
+
+    exe = ob.build_ref_host_loop()
+    if exe is None:
+        return None
+    raw = np.ascontiguousarray(case["raw"], np.complex64)
+    C_, S = raw.shape
+    grid = np.ascontiguousarray(case["grid"].reshape(-1, 3), np.float32)
+    import oracle
+
+    lam = float(oracle.wavelength_center(case["sample_times"], case["mod_rate"], case["start_freq"]))
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "img.bin"
+        with open(fin, "wb") as f:
+            f.write(np.array([C_, S, grid.shape[0]], np.int32).tobytes())
+            f.write(np.array([case["mod_rate"], case["start_freq"], lam, case["center"], case["bw"]],
+                             np.float32).tobytes())
+            f.write(np.array([case["centroid"], case["apply_range_win"], case["taper"]], np.int32).tobytes())
+            f.write(np.asarray(case["bore"], np.float32).tobytes())
+            f.write(raw.tobytes())
+            f.write(np.ascontiguousarray(case["sample_times"], np.float32).tobytes())
+            for k in ("pos", "vel", "att"):
+                f.write(np.ascontiguousarray(case[k], np.float32).tobytes())
+            f.write(grid.tobytes())
+        best = None
+        for _ in range(repeats):
+            r = subprocess.run([str(exe), str(ptx), str(fin), str(fout)], capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"ref_host_loop failed: {r.stderr[-2000:]}")
+            res = json.loads(r.stdout.strip().splitlines()[-1])
+            if best is None or res["ms"] < best["ms"]:
+                best = res
+        img = np.fromfile(fout, np.float32).view(np.complex64)
+    return best, img
 
 
 def main() -> int:
@@ -54,6 +101,7 @@ def main() -> int:
                 grid=flat[pix].astype(np.float32), mod_rate=np.float32(sc.radar.mod_rate),
                 start_freq=np.float32(sc.radar.f0), center=0.0, bw=float("inf"), centroid=0, apply_range_win=0,
                 taper=1, bore=np.array([0, 1, 0], np.float32))
+    host_loop = run_host_loop(case, Path(ptx))
     # infinite band: the host skip test passes every chunk; sums stay on the device
     ref.reference_focus(drv, dict(case, grid=case["grid"][:4]), host_skip=False, device_sum=True)  # warm-up
     torch.cuda.synchronize()
@@ -79,6 +127,18 @@ def main() -> int:
            "reference_kernels_full_image_s": round(per_px * flat.shape[0], 2),
            "engine_vs_reference_rel_l2": err,
            "launches_per_pixel": 3 * ((C_ + ref.CHUNK - 1) // ref.CHUNK)}
+    if host_loop is not None:
+        hl, img_hl = host_loop
+        per_px_hl = hl["ms"] / 1e3 / n_pix
+        out["host_loop"] = dict(hl, ms_per_pixel=round(per_px_hl * 1e3, 4),
+                                gcorr_s=round(C_ * S / per_px_hl / 1e9, 4),
+                                full_image_s=round(per_px_hl * flat.shape[0], 2),
+                                engine_vs_host_loop_rel_l2=float(np.linalg.norm(img - img_hl) /
+                                                                 np.linalg.norm(img_hl)),
+                                python_loop_vs_host_loop_rel_l2=float(np.linalg.norm(img_ref - img_hl) /
+                                                                      np.linalg.norm(img_hl)))
+    else:
+        out["host_loop"] = "unavailable: NPP headers or libraries missing on this machine"
     print(json.dumps(out))
     return 0
 

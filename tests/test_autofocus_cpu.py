@@ -79,3 +79,22 @@ def test_operator_refuses_paths_without_an_adjoint():
     p.path = lambda: "general"
     with pytest.raises(RuntimeError, match="FP32-bulk"):
         autofocus.FocusOperator(p)
+
+
+def test_hat_basis_interpolates_between_control_points():
+    import pytest
+    import torch
+
+    from sarlabtdc import autofocus
+
+    B = autofocus.hat_basis(101, 11, "cpu")
+    assert B.shape == (101, 11) and B.dtype == torch.float64
+    assert torch.allclose(B.sum(1), torch.ones(101, dtype=torch.float64))
+    # control point k sits on chirp 10 k; values between them are linear
+    theta = torch.arange(11, dtype=torch.float64) ** 2
+    v = B @ theta
+    for k in range(11):
+        assert float(v[10 * k]) == float(theta[k])
+    assert abs(float(v[5]) - 0.5 * (theta[0] + theta[1])) < 1e-12
+    with pytest.raises(ValueError):
+        autofocus.hat_basis(10, 11, "cpu")
