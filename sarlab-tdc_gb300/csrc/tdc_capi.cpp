@@ -89,6 +89,11 @@ constexpr double kGeneralNarrowCycles = 4.0;
 // Smooth-motion kernel: largest deviation of the per-sample phase correction from its
 // per-segment linear model (chord + mean offset) [rad].
 constexpr double kMotionTolRad = 2e-3;
+// Block tiles: kFocusTile / kBlockTileCols grid rows x kBlockTileCols columns.
+#ifndef TDC_BLOCK_TILES
+#define TDC_BLOCK_TILES 1
+#endif
+constexpr int kBlockTileCols = 16;
 #ifndef TDC_GENERAL_STAGE_TARGET
 #define TDC_GENERAL_STAGE_TARGET 32768
 #endif
@@ -314,14 +319,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
         for (int c = cb; c < ce; ++c) recs[c] = make_record(p, c, 0, o.centroid != 0, o.center);
     });
     p->sample_recs_ready = false;
-    // With an unbounded band the window is 1 wherever the range is positive, provided the
-    // velocities and window centres are finite (else the reference's window is NaN -> 0).
-    p->unit_window_ok = true;
-    for (int c = 0; c < C && p->unit_window_ok; ++c) {
-        const ChirpRec &r = recs[c];
-        p->unit_window_ok = std::isfinite(r.vel.x) && std::isfinite(r.vel.y) && std::isfinite(r.vel.z) &&
-                            std::isfinite(r.p_hi.w);
-    }
+    p->rec_host = recs;
     {
         double v[3] = {0.0, 0.0, 0.0};
         for (int c = 0; c < C; ++c) {
@@ -624,6 +622,28 @@ int upload_grid(tdc_processor *p, int &launches)
             p->axis_c[k] = p->cols > 1 ? g(1, k) - g(0, k) : 0.0;
             p->axis_r[k] = p->rows > 1 ? g(p->cols, k) - g(0, k) : 0.0;
         }
+        // centre pixel of every work tile, flat and block (the planner's cost estimate under
+        // a finite Doppler band)
+        p->tile_centre_flat.clear();
+        p->tile_centre_block.clear();
+        if (P > 0) {
+            const long long n_flat = (P + kFocusTile - 1) / kFocusTile;
+            p->tile_centre_flat.resize((size_t)n_flat * 3);
+            for (long long t = 0; t < n_flat; ++t) {
+                const long long i = std::min(P - 1, t * kFocusTile + kFocusTile / 2);
+                for (int k = 0; k < 3; ++k) p->tile_centre_flat[3 * t + k] = g(i, k);
+            }
+            const int tile_rows = kFocusTile / kBlockTileCols;
+            const long long n_tr = (p->rows + tile_rows - 1) / tile_rows;
+            const long long n_tc = (p->cols + kBlockTileCols - 1) / kBlockTileCols;
+            p->tile_centre_block.resize((size_t)(n_tr * n_tc) * 3);
+            for (long long tr = 0; tr < n_tr; ++tr)
+                for (long long tc = 0; tc < n_tc; ++tc) {
+                    const long long r = std::min<long long>(p->rows - 1, tr * tile_rows + tile_rows / 2);
+                    const long long c = std::min<long long>(p->cols - 1, tc * kBlockTileCols + kBlockTileCols / 2);
+                    for (int k = 0; k < 3; ++k) p->tile_centre_block[3 * (tr * n_tc + tc) + k] = g(r * p->cols + c, k);
+                }
+        }
     }
     if (!p->host_reads) {
         for (int k = 0; k < 3; ++k) {
@@ -773,11 +793,6 @@ int choose_path(const tdc_processor *p)
     return TDC_PATH_GENERAL;
 }
 
-// Block tiles: kFocusTile / kBlockTileCols grid rows x kBlockTileCols columns.
-#ifndef TDC_BLOCK_TILES
-#define TDC_BLOCK_TILES 1
-#endif
-constexpr int kBlockTileCols = 16;
 
 // With a finite Doppler band, chirps whose window (or chunk skip test) is zero for every
 // pixel of a warp skip their work, but a CTA's warps wait for one another at each pipeline
@@ -796,6 +811,44 @@ int choose_tile_cols(const tdc_processor *p)
         return n > 0.0 ? std::fabs(a[0] * p->vel_dir[0] + a[1] * p->vel_dir[1] + a[2] * p->vel_dir[2]) / n : 0.0;
     };
     return along(p->axis_c) > along(p->axis_r) ? kBlockTileCols : 0;
+}
+
+// Under a finite Doppler band a unit's cost follows its live chirps, which depend on where
+// its tile lies: the units are put in order of decreasing estimated cost (the window at the
+// tile's centre pixel for each chirp of the group), so the persistent CTAs take the long
+// ones first and the launch does not end on a few long units. Only the order in which CTAs
+// take units changes: each pixel's sums, and so the image, are the same.
+void order_units_by_cost(tdc_processor *p, int tile_cols)
+{
+    if (!std::isfinite(p->opts.bw) || p->rec_host.size() != (size_t)p->C || p->units_host.size() < 2) return;
+    const std::vector<double> &centres = tile_cols ? p->tile_centre_block : p->tile_centre_flat;
+    const long long n_tiles = (long long)centres.size() / 3;
+    const int C = p->C, cpg = p->plan_cpg, groups = p->plan_groups;
+    if ((long long)p->units_host.size() != n_tiles * groups) return;
+    const double two_over_lambda = 2.0 / (double)p->lambda, half_bw = 0.5 * (double)p->opts.bw;
+    std::vector<double> cost((size_t)n_tiles * groups, 0.0);
+    parallel_chirps((int)n_tiles, C, [&](int, int t0, int t1) {
+        for (int t = t0; t < t1; ++t) {
+            const double *T = &centres[3 * (size_t)t];
+            for (int g = 0; g < groups; ++g) {
+                const int c0 = g * cpg, c1 = std::min(C, c0 + cpg);
+                long live = 0;
+                for (int c = c0; c < c1; ++c) {
+                    const ChirpRec &r = p->rec_host[c];
+                    const double dx = ((double)r.p_hi.x + r.p_lo.x) - T[0], dy = ((double)r.p_hi.y + r.p_lo.y) - T[1],
+                                 dz = ((double)r.p_hi.z + r.p_lo.z) - T[2];
+                    const double n = std::sqrt(dx * dx + dy * dy + dz * dz);
+                    const double fd = -two_over_lambda * (r.vel.x * dx + r.vel.y * dy + r.vel.z * dz) / n;
+                    live += std::fabs(fd - (double)r.p_hi.w) <= half_bw ? 1 : 0;
+                }
+                // a live chirp costs its samples' MACs and the set-up, a dead one the vote
+                cost[(size_t)t * groups + g] = (double)live * (p->s_pad + 64) + (double)(c1 - c0 - live) * 24.0;
+            }
+        }
+    });
+    std::stable_sort(p->units_host.begin(), p->units_host.end(), [&](const FocusUnit &a, const FocusUnit &b) {
+        return cost[(size_t)a.tile * groups + a.group] > cost[(size_t)b.tile * groups + b.group];
+    });
 }
 
 // Split the chirps into groups so that tiles x groups units fill whole waves of `slots`;
@@ -932,7 +985,6 @@ FocusJob make_job(const tdc_processor *p, float4 *partial, int cb, int path)
     job.chunk = kChunk;
     job.stage_chirps = cb;
     job.flags = (p->opts.taper ? kFlagTaper : 0) | (p->opts.skip_test ? kFlagSkipTest : 0);
-    if (std::isinf(p->opts.bw) && p->opts.bw > 0.f && p->unit_window_ok) job.flags |= kFlagUnitWindow;
     job.n_tiles = (int)((p->P + kFocusTile - 1) / kFocusTile);
     job.per_sample = rec_per_sample ? 1 : 0;
     const double g0 = 2.0 * p->F0 / kC0, g1 = 2.0 * p->F1 / kC0;
@@ -1046,6 +1098,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         p->units_host.reserve((size_t)(n_tiles * p->plan_groups));
         for (long long t = 0; t < n_tiles; ++t)
             for (int g = 0; g < p->plan_groups; ++g) p->units_host.push_back(FocusUnit{0, (int)t, g, 0});
+        if (path != TDC_PATH_FP64_PHASE && path != TDC_PATH_GENERAL_FP64) order_units_by_cost(p, tile_cols);
         p->plan_path = path;
         p->plan_P = P;
         p->plan_C = C;

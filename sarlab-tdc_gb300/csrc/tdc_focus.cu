@@ -54,30 +54,6 @@ constexpr int kUnrollBlocks = TDC_FOCUS_UNROLL;
 #define TDC_FOCUS_EARLY_VOTE 1
 #endif
 constexpr bool kEarlyVote = TDC_FOCUS_EARLY_VOTE != 0;
-// Unbounded-band instance: skip the Doppler window arithmetic when the job says the window
-// is 1 wherever the range is positive (1), or evaluate it always (0).
-#ifndef TDC_FOCUS_UNIT_WINDOW
-#define TDC_FOCUS_UNIT_WINDOW 0
-#endif
-// Block step QL = e^{j 2 pi L beta}: from a 64-entry table of e^{j 2 pi k / 64} and a short
-// series for the remainder (1), or from an accurate sincospif (0).
-#ifndef TDC_FOCUS_QL_TABLE
-#define TDC_FOCUS_QL_TABLE 0
-#endif
-
-// e^{j 2 pi f} for |f| <= ~0.51 cycles: the table entry nearest f (multiples of 1/64) times
-// the series of the remainder (|2 pi r| <= 0.05 rad: error < 1e-10).
-__device__ __forceinline__ float2 phasor_from_table(const float2 *__restrict__ tab, float f)
-{
-    const float a = rintf(64.0f * f);
-    const int k = __float2int_rn(a) & 63;
-    const float t = kTwoPiF * fmaf(a, -1.0f / 64.0f, f);
-    const float t2 = t * t;
-    const float c = fmaf(t2, fmaf(t2, 1.0f / 24.0f, -0.5f), 1.0f);
-    const float sn = t * fmaf(t2, fmaf(t2, 1.0f / 120.0f, -1.0f / 6.0f), 1.0f);
-    const float2 e = tab[k];
-    return make_float2(fmaf(e.x, c, -e.y * sn), fmaf(e.x, sn, e.y * c));
-}
 
 struct SharedPixel {
     float t[kFocusPT * 6][kFocusThreads];  // (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo) per pixel slot
@@ -189,9 +165,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     __shared__ uint64_t full_bar[kFocusStages];
     __shared__ int s_unit;
     __shared__ FocusJob sJ;
-#if TDC_FOCUS_QL_TABLE
-    __shared__ float2 ql_tab[64];
-#endif
 
     SharedPixel &sp = *reinterpret_cast<SharedPixel *>(smem + kFocusStages * stage_bytes);
 
@@ -201,13 +174,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
         for (int i = 0; i < kFocusStages; ++i) mbar_init(&full_bar[i], 1);
         fence_barrier_init();
     }
-#if TDC_FOCUS_QL_TABLE
-    if (tid < 64) {
-        float s, c;
-        sincospif((float)tid / 32.0f, &s, &c);
-        ql_tab[tid] = make_float2(c, s);
-    }
-#endif
     __syncthreads();
 
     uint32_t n_issued = 0;    // producer (thread 0) only
@@ -277,7 +243,6 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
         const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
         const bool taper = (sJ.flags & kFlagTaper) != 0;
         const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
-        const bool unit_window = (sJ.flags & kFlagUnitWindow) != 0;
         const int chunk = sJ.chunk;
         const SkipPoint *__restrict__ skip = sJ.skip;
         const int nb = s_pad / kL;
@@ -387,20 +352,11 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                         for (int k = 1; k < kL - 1; ++k) p[i][k] = cmul(p[i][k - 1], p[i][0]);
                         const float lbh = (float)kL * bh;  // exact
                         const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
-#if TDC_FOCUS_QL_TABLE
-                        ql[i] = phasor_from_table(ql_tab, lfr);
-#else
                         float sl, cl;
                         sincospif(2.0f * lfr, &sl, &cl);
                         ql[i] = make_float2(cl, sl);
-#endif
-                        float w;
-                        if (TDC_FOCUS_UNIT_WINDOW && !SKIP_ZERO && unit_window) {
-                            w = dh > 0.0f ? wskip[i] : 0.0f;
-                        } else {
-                            const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
-                            w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
-                        }
+                        const float fd = doppler_freq(tol, r.vel.x, r.vel.y, r.vel.z, dxh, dyh, dzh, rs);
+                        const float w = wskip[i] * doppler_window(fd, r.p_hi.w, half_bw, inv_bw, taper, az_a);
                         if (SKIP_ZERO) live |= w != 0.0f;
                         float sa, ca;
                         __sincosf(kTwoPiF * alpha, &sa, &ca);

@@ -85,8 +85,6 @@ enum FocusFlags : int {
     kFlagTaper = 1,     // dopplerWinTaper
     kFlagSkipTest = 2,  // apply the per-chunk skip test
     kFlagMotionExactQL = 4,  // smooth-motion kernel: block step per segment from an accurate sincos
-    kFlagUnitWindow = 8,     // unbounded Doppler band with finite velocities and window centres: the
-                             // window is 1 wherever the range is positive (0 at R = 0, like the NaN window)
 };
 
 // Everything a focus kernel needs about one job (acquisition x grid).

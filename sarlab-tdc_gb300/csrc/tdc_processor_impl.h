@@ -158,7 +158,6 @@ struct tdc_processor {
     // Smooth intra-chirp motion: every chirp's per-sample positions are P0 + V1 s + V2 s^2 to
     // within the rounding of their FP32 values (motion_rec holds the fits); the smooth-motion
     // kernel then runs instead of the FP32 general kernel, unless switched off.
-    bool unit_window_ok = false;  // every chirp record's velocity and window centre are finite
     bool motion_fit_ok = false;
     bool motion_enabled = true;
     double motion_v1max = 0.0;  // max |V1| [m / sample]
@@ -187,6 +186,10 @@ struct tdc_processor {
     double axis_c[3] = {0, 0, 0}, axis_r[3] = {0, 0, 0};  // grid column / row steps (first pixel's)
     double vel_dir[3] = {0, 0, 0};                         // mean antenna velocity direction (0: at rest)
     tdc::impl::DevBuf grid_stage, grid_hi, grid_lo;
+    // Centre pixel (x, y, z) of each work tile, flat tiles and block tiles.
+    std::vector<double> tile_centre_flat, tile_centre_block;
+    // Host copy of the chirp records (sample 0), for the planner's cost estimate.
+    std::vector<tdc::ChirpRec> rec_host;
 
     // Focus plan cache + scratch.
     tdc::impl::DevBuf scratch;
