@@ -215,9 +215,10 @@ def test_kernels_compile_without_register_spills(engine_lib):
         assert m_sp and m_rg, name
         seen[name] = (int(m_sp.group(1)), int(m_sp.group(2)), int(m_rg.group(1)))
     hot = {n: v for n, v in seen.items()
-           if any(k in n for k in ("focus_fp32", "focus_general", "adjoint_fp32_kernel", "focus_fp64"))}
-    # 4 bulk + 2 segmented + 7 general + 2 FP64 + 2 adjoint instances
-    assert len(hot) >= 17, sorted(hot)
+           if any(k in n for k in ("focus_fp32", "focus_general", "focus_motion", "adjoint_fp32_kernel",
+                                   "focus_fp64"))}
+    # 4 bulk + 2 segmented + 7 general + 2 smooth-motion + 2 FP64 + 2 adjoint instances
+    assert len(hot) >= 19, sorted(hot)
     for name, (st, ld, regs) in hot.items():
         assert st == 0 and ld == 0, f"{name}: {st} B spill stores, {ld} B spill loads"
         assert regs <= 168 or "focus_fp64" in name, f"{name}: {regs} registers"
