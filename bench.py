@@ -726,13 +726,17 @@ def autofocus_leg(args):
     op.adjoint(zero, g)
     torch.cuda.synchronize()
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    e[0].record()
-    img = op.image(zero)
-    e[1].record()
-    op.adjoint(zero, g)
-    e[2].record()
-    torch.cuda.synchronize()
-    fwd_ms, adj_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    fwd_runs, adj_runs = [], []
+    for _ in range(5):
+        e[0].record()
+        img = op.image(zero)
+        e[1].record()
+        op.adjoint(zero, g)
+        e[2].record()
+        torch.cuda.synchronize()
+        fwd_runs.append(e[0].elapsed_time(e[1]))
+        adj_runs.append(e[1].elapsed_time(e[2]))
+    fwd_ms, adj_ms = float(np.median(fwd_runs)), float(np.median(adj_runs))
     adj_kept = bool(p.lastStats()["adjoint_stored"])
     # the same adjoint recomputing the forward's sums instead of reading them
     p.keepChirpSums(False)

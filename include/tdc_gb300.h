@@ -143,6 +143,9 @@ typedef struct tdc_start_stats {
                              grid's columns) */
     int adjoint_stored;   /* the last adjoint read the kept per-chirp sums (1) or recomputed them (0) */
     int motion_segment;   /* smooth-motion path: samples per linearised segment; 0 on the other paths */
+    int anchor_pixels;    /* FP32-bulk path with anchored ranges: consecutive pixels sharing one anchor
+                             (32); 0 when every pixel's range is formed in double-float */
+    int reserved;
 } tdc_start_stats;
 
 typedef enum tdc_path {
@@ -183,6 +186,17 @@ int tdc_processor_set_plan_pixels(tdc_processor *proc, int64_t n_pix);
  * the FP32 general kernel). Extension without a reference counterpart; takes effect at the
  * next focus. */
 int tdc_processor_set_motion_path(tdc_processor *proc, int enable);
+
+/* Anchored ranges in the FP32-bulk kernel on (1, default) or off (0). With an unbounded Doppler
+ * band, finite velocities, no kept per-chirp sums and rows of 3-16 chirps per pipeline stage
+ * (about 128-700 samples), groups of 32 consecutive pixels share an anchor pixel whose
+ * range and phase terms are formed in double-float once per chirp; each pixel adds its range
+ * difference from the anchor in FP32 (exact in form: d.(d - 2e) / (R0 + R), no cancellation).
+ * Taken only when no pixel lies farther than 5 cm from its anchor (grids whose rows are a
+ * multiple of 32 pixels, or narrower than 5 cm, at up to 3 mm spacing), which keeps the phase
+ * within about 2e-5 rad of the per-pixel double-float range's. Off: every (pixel, chirp) range
+ * in double-float. Extension without a reference counterpart; takes effect at the next focus. */
+int tdc_processor_set_anchored_ranges(tdc_processor *proc, int enable);
 
 /*
  * The parts of start() before the per-pixel work, leaving the acquisition

@@ -216,6 +216,13 @@ class TdcProcessor:
         smooth-motion kernel (default) or, when off, the FP32 general kernel."""
         _lib.check(_lib.lib().tdc_processor_set_motion_path(self._h, int(bool(enable))))
 
+    def setAnchoredRanges(self, enable: bool):
+        """Extension: with an unbounded Doppler band, groups of consecutive pixels share a
+        double-float anchor range per chirp and add their FP32 range differences (default on;
+        taken when every pixel lies within 5 cm of its anchor). Off: every (pixel, chirp)
+        range in double-float."""
+        _lib.check(_lib.lib().tdc_processor_set_anchored_ranges(self._h, int(bool(enable))))
+
     def setSkipTest(self, enable: bool):
         _lib.check(_lib.lib().tdc_processor_set_skip_test(self._h, int(bool(enable))))
 

@@ -125,6 +125,8 @@ class StartStats(C.Structure):
         ("tile_cols", C.c_int),
         ("adjoint_stored", C.c_int),
         ("motion_segment", C.c_int),
+        ("anchor_pixels", C.c_int),
+        ("reserved", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -157,6 +159,7 @@ SIGNATURES = [
     ("tdc_range_window", C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     ("tdc_processor_set_skip_test", C.c_int, [_vp, C.c_int]),
     ("tdc_processor_set_motion_path", C.c_int, [_vp, C.c_int]),
+    ("tdc_processor_set_anchored_ranges", C.c_int, [_vp, C.c_int]),
     ("tdc_processor_set_plan_pixels", C.c_int, [_vp, C.c_int64]),
     ("tdc_processor_prepare", C.c_int, [_vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]),
     ("tdc_processor_upload_grid", C.c_int, [_vp]),

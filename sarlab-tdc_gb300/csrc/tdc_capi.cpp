@@ -89,6 +89,10 @@ constexpr double kGeneralNarrowCycles = 4.0;
 // Smooth-motion kernel: largest deviation of the per-sample phase correction from its
 // per-segment linear model (chord + mean offset) [rad].
 constexpr double kMotionTolRad = 2e-3;
+// Work of one unit (tile x chirp group) the planner aims at in long launches [correlations]:
+// a few milliseconds of a CTA's time (measured: 16-64 units per slot take 533 ms instead of
+// 538.6 ms on 1024^2 x 4096 x 1024; at 4.5 ms launches more units cost 2-8%).
+constexpr double kUnitTargetCorr = 64e6;
 // Block tiles: kFocusTile / kBlockTileCols grid rows x kBlockTileCols columns.
 #ifndef TDC_BLOCK_TILES
 #define TDC_BLOCK_TILES 1
@@ -320,6 +324,10 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     });
     p->sample_recs_ready = false;
     p->rec_host = recs;
+    p->rec_finite = true;
+    for (int c = 0; c < C; ++c)
+        p->rec_finite = p->rec_finite && std::isfinite(recs[c].vel.x) && std::isfinite(recs[c].vel.y) &&
+                        std::isfinite(recs[c].vel.z) && std::isfinite(recs[c].p_hi.w);
     {
         double v[3] = {0.0, 0.0, 0.0};
         for (int c = 0; c < C; ++c) {
@@ -633,6 +641,19 @@ int upload_grid(tdc_processor *p, int &launches)
                 const long long i = std::min(P - 1, t * kFocusTile + kFocusTile / 2);
                 for (int k = 0; k < 3; ++k) p->tile_centre_flat[3 * t + k] = g(i, k);
             }
+            // anchored ranges: distance of each pixel from its group's anchor (groups of 32
+            // consecutive pixels; the anchor is the 17th pixel or the group's last)
+            double span2 = 0.0;
+            for (long long b = 0; b < P; b += 32) {
+                const long long a = std::min(P - 1, b + 16);
+                const double ax = g(a, 0), ay = g(a, 1), az = g(a, 2);
+                for (long long i = b; i < std::min(P, b + 32); ++i) {
+                    const double dx = g(i, 0) - ax, dy = g(i, 1) - ay, dz = g(i, 2) - az;
+                    const double d2 = dx * dx + dy * dy + dz * dz;
+                    span2 = d2 > span2 || d2 != d2 ? d2 : span2;
+                }
+            }
+            p->anchor_span = std::sqrt(span2);
             const int tile_rows = kFocusTile / kBlockTileCols;
             const long long n_tr = (p->rows + tile_rows - 1) / tile_rows;
             const long long n_tc = (p->cols + kBlockTileCols - 1) / kBlockTileCols;
@@ -904,7 +925,7 @@ int stage_bytes_for(int s_pad, int &cb)
 
 bool needs_segments(int s_pad)
 {
-    return focus_fp32_smem_bytes(0) + kFocusStages * (int)round_up((size_t)s_pad * 8 + sizeof(ChirpRec), 128) >
+    return focus_fp32_smem_bytes(0, false) + kFocusStages * (int)round_up((size_t)s_pad * 8 + sizeof(ChirpRec), 128) >
            226 * 1024;
 }
 
@@ -1019,6 +1040,23 @@ int sample_records(tdc_processor *p)
     return TDC_OK;
 }
 
+// Anchored ranges for an FP32-bulk focus staged whole, cb chirps a stage: the plain kernel
+// instance (unbounded band, so flat tiles; no kept per-chirp sums) with finite velocities and
+// window centres (the instance then forms no Doppler window), 3 to kAnchorMaxStageChirps
+// chirps a stage (with fewer, a pass of the warp's lanes over a stage's anchor records costs
+// about what the pixels save: S = 1024 measured 0.4% slower), every pixel within
+// kAnchorMaxDistance of its anchor, and the block step's correction 2 pi L g1 |dR| within its
+// series' range (0.8 rad).
+bool anchor_eligible(const tdc_processor *p, int cb)
+{
+    if (!p->anchor_enabled || p->keep_sums || !p->per_chirp || !p->rec_finite) return false;
+    if (std::isfinite(p->opts.bw / 2.0f)) return false;
+    if (cb < 3 || cb > kAnchorMaxStageChirps) return false;
+    if (!(p->anchor_span <= kAnchorMaxDistance)) return false;
+    const double g1 = 2.0 * p->F1 / kC0;
+    return 2.0 * M_PI * 8.0 * std::fabs(g1) * p->anchor_span <= 0.8;
+}
+
 int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
 {
     if (!p->prepared) return fail(TDC_ERR_STATE, "acquisition not prepared");
@@ -1054,6 +1092,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     // to 0.8 rad, else an accurate sincos per segment
     const bool motion_exact_ql = path == TDC_PATH_FP32_MOTION && !(2.0 * M_PI * 8.0 * motion_slope_bound(p) <= 0.8);
     int slots;
+    bool anchored = false;
     if (path == TDC_PATH_FP32_MOTION) {
         const int bps = focus_motion_blocks_per_sm(stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "smooth-motion focus kernel does not fit on the device");
@@ -1062,6 +1101,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         const int bps = seg ? focus_fp32_seg_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "focus kernel does not fit on the device");
         slots = p->n_sm * bps;
+        anchored = !seg && anchor_eligible(p, cb) && focus_fp32_anchor_blocks_per_sm(stage_bytes) >= bps;
     } else if (path == TDC_PATH_GENERAL) {
         const int bps = focus_general_blocks_per_sm(variant, stage_bytes);
         if (bps <= 0) return fail(TDC_ERR_CUDA, "general focus kernel does not fit on the device");
@@ -1080,8 +1120,17 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     if (path != p->plan_path || P != p->plan_P || C != p->plan_C || slots != p->plan_slots ||
         max_unit_work != p->plan_unit_cap || tile_cols != p->plan_tile_cols || plan_cols != p->plan_cols ||
         plan_tiles != p->plan_tiles) {
-        plan_groups(plan_tiles, C, slots, p->plan_groups, p->plan_cpg,
-                    path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot);
+        int min_units = path == TDC_PATH_GENERAL ? kGeneralMinUnitsPerSlot : kFocusMinUnitsPerSlot;
+        if (path == TDC_PATH_FP32_BULK && max_unit_work <= 0) {
+            // Long launches end on their last units: units of about kUnitTargetCorr correlations
+            // (up to 32 per CTA slot) shorten that tail; short launches keep fewer, larger units.
+            // (Request-loop launches bound their units by max_unit_work instead: finer units there
+            // delayed each request's completion.)
+            const double work = (double)plan_tiles * kFocusTile * C * p->s_pad;
+            const double by_work = std::floor(work / ((double)slots * kUnitTargetCorr));
+            min_units = std::max(min_units, (int)std::min(32.0, by_work));
+        }
+        plan_groups(plan_tiles, C, slots, p->plan_groups, p->plan_cpg, min_units);
         p->plan_tiles = plan_tiles;
         if (max_unit_work > 0) {
             // bound the work of one unit (tile x chirp group): at most cap / (tile x S) chirps per group
@@ -1118,6 +1167,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
     plan.cb = cb;
     plan.stage_bytes = stage_bytes;
     plan.slots = slots;
+    plan.anchored = anchored;
     plan.off_job = L.off_job;
     plan.off_units = L.off_units;
     plan.job = make_job(p, reinterpret_cast<float4 *>(scr + L.off_partial), cb, path);
@@ -1213,7 +1263,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
                    "focus kernel (segmented rows)");
         else
             TDC_CK(launch_focus_fp32(jobs_dev, units_dev, n_units, counter, status, stage_bytes, grid, skip_zero,
-                                     store, st),
+                                     store, plan.anchored && !skip_zero && !store, st),
                    "focus kernel");
     } else if (path == TDC_PATH_GENERAL) {
         const int grid = std::min(n_units, slots);
@@ -1240,6 +1290,10 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     p->stats.general_variant = path == TDC_PATH_GENERAL ? plan.variant : 0;
     p->stats.tile_cols = job.tile_cols;
     p->stats.motion_segment = path == TDC_PATH_FP32_MOTION ? job.seg_len : 0;
+    p->stats.anchor_pixels = 0;
+    if (path == TDC_PATH_FP32_BULK && !plan.seg && plan.anchored && !store && !std::isfinite(job.half_bw) &&
+        job.tile_cols == 0)
+        p->stats.anchor_pixels = 32;
     return TDC_OK;
 }
 
@@ -1248,6 +1302,7 @@ int read_status(tdc_processor *p)
     int status = 0;
     TDC_CK(cudaMemcpy(&status, p->scratch.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost), "read status");
     if (status & kStatusTimeout) return fail(TDC_ERR_TIMEOUT, "focus kernel wait timed out");
+    if (status & kStatusBadJob) return fail(TDC_ERR_CUDA, "focus kernel rejected its job record");
     return TDC_OK;
 }
 
@@ -1429,6 +1484,14 @@ int tdc_processor_set_motion_path(tdc_processor *p, int enable)
 {
     if (int rc = check_proc(p)) return rc;
     p->motion_enabled = enable != 0;
+    return TDC_OK;
+}
+
+int tdc_processor_set_anchored_ranges(tdc_processor *p, int enable)
+{
+    if (int rc = check_proc(p)) return rc;
+    p->anchor_enabled = enable != 0;
+    p->plan_path = -1;  // the anchored instance may change the planned CTA slots
     return TDC_OK;
 }
 

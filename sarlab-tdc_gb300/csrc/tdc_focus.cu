@@ -59,9 +59,38 @@ struct SharedPixel {
     float t[kFocusPT * 6][kFocusThreads];  // (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo) per pixel slot
 };
 
+// Anchored ranges (flat tiles, unbounded band). The 32 consecutive pixels of one warp and
+// slot share an anchor pixel, their 17th (or their last inside the grid). Per chirp, one lane
+// forms the anchor's range R0, start phase alpha0 = frac(g0 R0), per-sample step
+// beta0 = frac(g1 R0) and block step QL0 = e^{j 2 pi L beta0} in double-float (a stage's
+// 4 slots x chirps anchor records take one or two passes of the warp's lanes); a pixel then
+// needs only its range difference dR = R - R0 = d.(d - 2e) / (R0 + R) in FP32 (d = pixel -
+// anchor, e = antenna - anchor: no cancellation, |dR| <= |d|) and small corrections
+// alpha0 + g0 dR, beta0 + g1 dR, QL0 e^{j 2 pi L g1 dR}. With an unbounded band and finite
+// velocities and window centres, a chirp's window weight is 1 (0 where the antenna sits on the
+// pixel: NaN Doppler), so this instance forms no Doppler frequency. Its chirp sums q0 H go
+// into a per-stage sum by complex FMA, and the stage sums into the Kahan-compensated sum.
+constexpr int kAnchorRecs = kFocusPT * kAnchorMaxStageChirps;  // anchor records per warp and stage
+struct SharedAnchor {
+    float4 d[kFocusPT][kFocusThreads];              // pixel - anchor per slot (x, y, z, 0)
+    float anc[kFocusThreads / 32][kFocusPT][6];      // anchor per (warp, slot): hi xyz, lo xyz
+    float4 rec[kFocusThreads / 32][kAnchorRecs][2];  // per (chirp, slot): (e, R0), (alpha0, beta0, QL0)
+};
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// Kahan: comp carries the rounding error of the running sum (true = sum - comp).
+__device__ __forceinline__ void kahan_add(float2 &sum, float2 &comp, float2 v)
+{
+    const float yr = v.x - comp.x, yi = v.y - comp.y;
+    const float tr = sum.x + yr, ti = sum.y + yi;
+    comp.x = (tr - sum.x) - yr;
+    comp.y = (ti - sum.y) - yi;
+    sum.x = tr;
+    sum.y = ti;
 }
 
 // One Horner block for one pixel: H <- H * ql + sum_{k<L} x_k p_k (p_0 = 1).
@@ -156,19 +185,24 @@ __device__ __forceinline__ bool unit_pixel_ok(long long p, long long P)
 // plain instance keeps the hot loop's schedule).
 // STORE: also write each (pixel, chirp) sum A = sum_s x_s z^s (before the start phasor q0) to
 // job.chirp_sums[c][p], zero for chirps skipped by the window vote (the adjoint reads them).
-template <bool SKIP_ZERO, bool STORE>
+// ANCHOR: anchored ranges (SharedAnchor); flat tiles and an unbounded band only, stages of at
+// most kAnchorMaxStageChirps chirps, pixels within the host's anchor distance bound.
+template <bool SKIP_ZERO, bool STORE, bool ANCHOR = false>
 __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
     focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
                       int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
 {
+    static_assert(!ANCHOR || (!SKIP_ZERO && !STORE), "anchored ranges: plain instance only");
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full_bar[kFocusStages];
     __shared__ int s_unit;
     __shared__ FocusJob sJ;
 
     SharedPixel &sp = *reinterpret_cast<SharedPixel *>(smem + kFocusStages * stage_bytes);
+    SharedAnchor &sa = *reinterpret_cast<SharedAnchor *>(smem + kFocusStages * stage_bytes);
 
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
         for (int i = 0; i < kFocusStages; ++i) mbar_init(&full_bar[i], 1);
@@ -202,6 +236,13 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
         const float4 *__restrict__ xw = sJ.xw;
         const ChirpRec *__restrict__ chirps = sJ.chirps;
 
+        if (ANCHOR && kFocusPT * CB > kAnchorRecs) {
+            // more anchor records a stage than the shared buffer holds (the host never plans
+            // this): report, before any copy of this unit is issued
+            if (tid == 0) atomicOr(status, kStatusBadJob);
+            break;
+        }
+
         // Producer: issue the first stages of this unit (every warp is past the previous
         // unit's last stage: the buffers are free).
         if (tid == 0) {
@@ -220,26 +261,64 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
             }
         }
 
-        // Pixel coordinates of this thread's PT slots -> shared (own column).
         const long long P = sJ.P;
-#pragma unroll
-        for (int i = 0; i < kFocusPT; ++i) {
-            const long long p = unit_pixel<SKIP_ZERO>(sJ, P, un.tile, i * kFocusThreads + tid);
-            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
-            if (unit_pixel_ok<SKIP_ZERO>(p, P)) {
-                hi = __ldg(&sJ.grid_hi[p]);
-                if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[p]);
+        if constexpr (ANCHOR) {
+            // Anchor of slot i (lane i): the 17th pixel of the warp's 32, or the last inside the
+            // grid; none for 32 pixels wholly past the grid's end.
+            if (lane < kFocusPT) {
+                const int i = lane;
+                const long long base = (long long)un.tile * kFocusTile + i * kFocusThreads + warp * 32;
+                const long long n_valid = min(32LL, P - base);
+                float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+                if (n_valid > 0) {
+                    const long long a = base + min(16LL, n_valid - 1);
+                    hi = __ldg(&sJ.grid_hi[a]);
+                    if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[a]);
+                }
+                float *A = sa.anc[warp][lane];
+                A[0] = hi.x;
+                A[1] = hi.y;
+                A[2] = hi.z;
+                A[3] = lo.x;
+                A[4] = lo.y;
+                A[5] = lo.z;
             }
-            sp.t[i * 6 + 0][tid] = hi.x;
-            sp.t[i * 6 + 1][tid] = hi.y;
-            sp.t[i * 6 + 2][tid] = hi.z;
-            sp.t[i * 6 + 3][tid] = lo.x;
-            sp.t[i * 6 + 4][tid] = lo.y;
-            sp.t[i * 6 + 5][tid] = lo.z;
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < kFocusPT; ++i) {
+                const long long p = (long long)un.tile * kFocusTile + i * kFocusThreads + tid;
+                float4 dv = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (p < P) {
+                    const float4 hi = __ldg(&sJ.grid_hi[p]);
+                    const float4 lo = sJ.grid_lo ? __ldg(&sJ.grid_lo[p]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float *A = sa.anc[warp][i];
+                    dv = make_float4((hi.x - A[0]) + (lo.x - A[3]), (hi.y - A[1]) + (lo.y - A[4]),
+                                     (hi.z - A[2]) + (lo.z - A[5]), 0.f);
+                }
+                sa.d[i][tid] = dv;
+            }
+        } else {
+            // Pixel coordinates of this thread's PT slots -> shared (own column).
+#pragma unroll
+            for (int i = 0; i < kFocusPT; ++i) {
+                const long long p = unit_pixel<SKIP_ZERO>(sJ, P, un.tile, i * kFocusThreads + tid);
+                float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+                if (unit_pixel_ok<SKIP_ZERO>(p, P)) {
+                    hi = __ldg(&sJ.grid_hi[p]);
+                    if (sJ.grid_lo) lo = __ldg(&sJ.grid_lo[p]);
+                }
+                sp.t[i * 6 + 0][tid] = hi.x;
+                sp.t[i * 6 + 1][tid] = hi.y;
+                sp.t[i * 6 + 2][tid] = hi.z;
+                sp.t[i * 6 + 3][tid] = lo.x;
+                sp.t[i * 6 + 4][tid] = lo.y;
+                sp.t[i * 6 + 5][tid] = lo.z;
+            }
         }
 
         const float g0h = sJ.g0_hi, g0l = sJ.g0_lo, g1 = sJ.g1;
         const float g1l = sJ.g1_lo;
+        const float kql = kTwoPiF * (float)kL * g1;  // block step phase per metre of dR (anchored)
         const float tol = sJ.two_over_lambda, half_bw = sJ.half_bw, inv_bw = sJ.inv_bw, az_a = sJ.az_a;
         const bool taper = (sJ.flags & kFlagTaper) != 0;
         const bool skip_test = (sJ.flags & kFlagSkipTest) != 0;
@@ -265,7 +344,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 if (unit_pixel_ok<SKIP_ZERO>(px, P)) out[px] = a[i];
             }
         };
-        int cur_chunk = -1;
+        int chunk_end = 0;  // first chirp past the skip-test chunk of wskip
         bool timed_out = false;
 
         for (int j = 0; j < nblk; ++j) {
@@ -281,20 +360,62 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
             const ChirpRec *recs = reinterpret_cast<const ChirpRec *>(base + CB * row_bytes);
             const int cb0 = c0 + j * CB;
             const int cnt = min(CB, c1 - cb0);
+            float2 ssum[kFocusPT];  // this stage's chirp sums (anchored instance)
+#pragma unroll
+            for (int i = 0; i < kFocusPT; ++i) ssum[i] = make_float2(0.f, 0.f);
+
+            if constexpr (ANCHOR) {
+                // The stage's anchor records, record k = chirp x 4 + slot, from the staged chirp
+                // records (forming them for several stages at a time from the records in global
+                // memory measured 2-3.5% slower: every warp of the CTA waits on those loads).
+                for (int k = lane; k < kFocusPT * cnt; k += 32) {
+                    const ChirpRec r = recs[k >> 2];
+                    const float *A = sa.anc[warp][k & (kFocusPT - 1)];
+                    float exh, exl, eyh, eyl, ezh, ezl;
+                    dd_sub(r.p_hi.x, r.p_lo.x, A[0], A[3], exh, exl);
+                    dd_sub(r.p_hi.y, r.p_lo.y, A[1], A[4], eyh, eyl);
+                    dd_sub(r.p_hi.z, r.p_lo.z, A[2], A[5], ezh, ezl);
+                    float rh, rl, rs, dh;
+                    dd_range(exh, exl, eyh, eyl, ezh, ezl, rh, rl, rs, dh);
+                    const float alpha0 = dd_frac_mul(g0h, g0l, rh, rl);
+                    float bh = g1 * rh;
+                    float bl = fmaf(g1, rh, -bh);
+                    bl = fmaf(g1, rl, bl);
+                    bl = fmaf(g1l, rh, bl);
+                    bh -= rintf(bh);
+                    const float lbh = (float)kL * bh;  // exact
+                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
+                    float sl, cl;
+                    sincospif(2.0f * lfr, &sl, &cl);
+                    sa.rec[warp][k][0] = make_float4(exh + exl, eyh + eyl, ezh + ezl, rh + rl);
+                    sa.rec[warp][k][1] = make_float4(alpha0, bh + bl, cl, sl);
+                }
+                __syncwarp();
+            }
 
             for (int cc = 0; cc < cnt; ++cc) {
                 const int c = cb0 + cc;
-                if (skip_test) {
+                if (skip_test && c >= chunk_end) {
+                    // (chirps of a unit come in increasing order)
                     const int k = c / chunk;
-                    if (k != cur_chunk) {
-                        cur_chunk = k;
+                    chunk_end = (k + 1) * chunk;
+                    {
 #pragma unroll
                         for (int i = 0; i < kFocusPT; ++i) {
-                            wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, sp.t[i * 6 + 0][tid],
-                                                        sp.t[i * 6 + 1][tid], sp.t[i * 6 + 2][tid], tol,
-                                                        half_bw)
-                                           ? 1.0f
-                                           : 0.0f;
+                            float tx, ty, tz;
+                            if constexpr (ANCHOR) {
+                                // (the anchored instance keeps no pixel coordinates in shared memory)
+                                const long long px = (long long)un.tile * kFocusTile + i * kFocusThreads + tid;
+                                const float4 hi = px < P ? __ldg(&sJ.grid_hi[px]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                                tx = hi.x;
+                                ty = hi.y;
+                                tz = hi.z;
+                            } else {
+                                tx = sp.t[i * 6 + 0][tid];
+                                ty = sp.t[i * 6 + 1][tid];
+                                tz = sp.t[i * 6 + 2][tid];
+                            }
+                            wskip[i] = chunk_is_nonzero(skip + (size_t)k * 9, tx, ty, tz, tol, half_bw) ? 1.0f : 0.0f;
                         }
                     }
                 }
@@ -303,7 +424,41 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
 
                 float2 p[kFocusPT][kL - 1];
                 float2 ql[kFocusPT], q0[kFocusPT], h[kFocusPT];
-                if (SKIP_ZERO && kEarlyVote) {
+                if constexpr (ANCHOR) {
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) {
+                        const float4 dd = sa.d[i][tid];
+                        const int k = cc * kFocusPT + i;
+                        const float4 e = sa.rec[warp][k][0], a1 = sa.rec[warp][k][1];
+                        // antenna - pixel, and R^2 - R0^2 = d.(d - 2e)
+                        const float dvx = e.x - dd.x, dvy = e.y - dd.y, dvz = e.z - dd.z;
+                        float num = dd.x * fmaf(-2.0f, e.x, dd.x);
+                        num = fmaf(dd.y, fmaf(-2.0f, e.y, dd.y), num);
+                        num = fmaf(dd.z, fmaf(-2.0f, e.z, dd.z), num);
+                        const float r2 = fmaf(dvx, dvx, fmaf(dvy, dvy, dvz * dvz));
+                        const float rs = rsqrtf(r2);
+                        const float rr = r2 > 0.0f ? r2 * rs : 0.0f;
+                        const float den = e.w + rr;
+                        const float dr = den > 0.0f ? __fdividef(num, den) : 0.0f;
+                        const float w = r2 > 0.0f ? wskip[i] : 0.0f;
+                        // start phase alpha0 + g0 dR modulo one cycle (te: the product's rounding and g0's
+                        // low part)
+                        const float t = g0h * dr;
+                        const float te = fmaf(g0l, dr, fmaf(g0h, dr, -t));
+                        float a = (t - rintf(t)) + a1.x;
+                        a = (a - rintf(a)) + te;
+                        float sa0, ca0;
+                        __sincosf(kTwoPiF * a, &sa0, &ca0);
+                        q0[i] = make_float2(w * ca0, w * sa0);
+                        float s1, c1s;
+                        __sincosf(kTwoPiF * fmaf(g1, dr, a1.y), &s1, &c1s);
+                        p[i][0] = make_float2(c1s, s1);
+#pragma unroll
+                        for (int q = 1; q < kL - 1; ++q) p[i][q] = cmul(p[i][q - 1], p[i][0]);
+                        ql[i] = cmul(make_float2(a1.z, a1.w), sincos_small(kql * dr));
+                        h[i] = make_float2(0.f, 0.f);
+                    }
+                } else if (SKIP_ZERO && kEarlyVote) {
                     // Ranges and windows first: a chirp whose window (Doppler band, skip test) is
                     // zero for every pixel of the warp contributes nothing, and skips the phase
                     // set-up as well as the Horner loop.
@@ -381,17 +536,22 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 }
 
                 if (STORE) store_sums(c, h[0], h[1], h[2], h[3]);
+                if constexpr (ANCHOR) {
 #pragma unroll
-                for (int i = 0; i < kFocusPT; ++i) {
-                    const float2 v = cmul(q0[i], h[i]);
-                    // Kahan: comp carries the rounding error of the running sum (true = sum - comp).
-                    const float yr = v.x - comp[i].x, yi = v.y - comp[i].y;
-                    const float tr = sum[i].x + yr, ti = sum[i].y + yi;
-                    comp[i].x = (tr - sum[i].x) - yr;
-                    comp[i].y = (ti - sum[i].y) - yi;
-                    sum[i].x = tr;
-                    sum[i].y = ti;
+                    for (int i = 0; i < kFocusPT; ++i) {
+                        ssum[i].x = fmaf(q0[i].x, h[i].x, ssum[i].x);
+                        ssum[i].x = fmaf(-q0[i].y, h[i].y, ssum[i].x);
+                        ssum[i].y = fmaf(q0[i].x, h[i].y, ssum[i].y);
+                        ssum[i].y = fmaf(q0[i].y, h[i].x, ssum[i].y);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < kFocusPT; ++i) kahan_add(sum[i], comp[i], cmul(q0[i], h[i]));
                 }
+            }
+            if constexpr (ANCHOR) {
+#pragma unroll
+                for (int i = 0; i < kFocusPT; ++i) kahan_add(sum[i], comp[i], ssum[i]);
             }
 
             __syncthreads();  // every thread is done with this stage
@@ -673,14 +833,25 @@ __global__ void focus_reduce_kernel(const float4 *__restrict__ partial, int n_gr
 
 }  // namespace
 
-int focus_fp32_smem_bytes(int stage_bytes)
+int focus_fp32_smem_bytes(int stage_bytes, bool anchored)
 {
-    return kFocusStages * stage_bytes + (int)sizeof(SharedPixel);
+    return kFocusStages * stage_bytes + (int)(anchored ? sizeof(SharedAnchor) : sizeof(SharedPixel));
+}
+
+int focus_fp32_anchor_blocks_per_sm(int stage_bytes)
+{
+    const int smem = focus_fp32_smem_bytes(stage_bytes, true);
+    int blocks = 0;
+    if (allow_max_dynamic_smem(focus_fp32_kernel<false, false, true>) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel<false, false, true>, kFocusThreads,
+                                                      smem) != cudaSuccess)
+        return 0;
+    return blocks;
 }
 
 int focus_fp32_blocks_per_sm(int stage_bytes)
 {
-    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    const int smem = focus_fp32_smem_bytes(stage_bytes, false);
     int best = 1 << 30;
     for (auto fn : {focus_fp32_kernel<false, false>, focus_fp32_kernel<true, false>, focus_fp32_kernel<false, true>,
                     focus_fp32_kernel<true, true>}) {
@@ -695,12 +866,14 @@ int focus_fp32_blocks_per_sm(int stage_bytes)
 
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units, int *counter_dev,
                               int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero, bool store_sums,
-                              cudaStream_t st)
+                              bool anchored, cudaStream_t st)
 {
-    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    if (anchored && (skip_zero || store_sums)) return cudaErrorInvalidValue;
+    const int smem = focus_fp32_smem_bytes(stage_bytes, anchored);
     using Fn = void (*)(const FocusJob *, const FocusUnit *, int, int *, int *, int);
-    const Fn fn = skip_zero ? (store_sums ? focus_fp32_kernel<true, true> : focus_fp32_kernel<true, false>)
-                            : (store_sums ? focus_fp32_kernel<false, true> : focus_fp32_kernel<false, false>);
+    const Fn fn = anchored    ? focus_fp32_kernel<false, false, true>
+                  : skip_zero ? (store_sums ? focus_fp32_kernel<true, true> : focus_fp32_kernel<true, false>)
+                              : (store_sums ? focus_fp32_kernel<false, true> : focus_fp32_kernel<false, false>);
     cudaError_t e = allow_max_dynamic_smem(fn);
     if (e != cudaSuccess) return e;
     fn<<<grid_ctas, kFocusThreads, smem, st>>>(jobs_dev, units_dev, n_units, counter_dev, status_dev, stage_bytes);
@@ -709,7 +882,7 @@ cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_d
 
 int focus_fp32_seg_blocks_per_sm(int stage_bytes)
 {
-    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    const int smem = focus_fp32_smem_bytes(stage_bytes, false);
     int blocks = 0, blocks_skip = 0;
     if (allow_max_dynamic_smem(focus_fp32_seg_kernel<false>) != cudaSuccess ||
         allow_max_dynamic_smem(focus_fp32_seg_kernel<true>) != cudaSuccess)
@@ -726,7 +899,7 @@ cudaError_t launch_focus_fp32_seg(const FocusJob *jobs_dev, const FocusUnit *uni
                                   int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas, bool skip_zero,
                                   cudaStream_t st)
 {
-    const int smem = focus_fp32_smem_bytes(stage_bytes);
+    const int smem = focus_fp32_smem_bytes(stage_bytes, false);
     cudaError_t e = skip_zero ? allow_max_dynamic_smem(focus_fp32_seg_kernel<true>)
                               : allow_max_dynamic_smem(focus_fp32_seg_kernel<false>);
     if (e != cudaSuccess) return e;

@@ -28,6 +28,12 @@ constexpr int kSampleAlign = 16;  // s_pad is a multiple of this (bulk-copy rows
 #define TDC_FOCUS_STAGE_TARGET 16640
 #endif
 constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp rows + records per pipeline stage
+// Anchored ranges of the FP32-bulk kernel (pixels of a warp share a double-float anchor
+// range per chirp, each adds its FP32 range difference): at most this many chirps per stage,
+// and no pixel farther than kAnchorMaxDistance from its anchor. At 5 cm the FP32 range
+// difference keeps the phase within ~2e-5 rad of the double-float range's at 77 GHz.
+constexpr int kAnchorMaxStageChirps = 16;
+constexpr double kAnchorMaxDistance = 0.05;  // metres
 // Fewest work units per CTA slot the planner aims for where the grid and chirps allow
 // it. CTAs that share an SM need not progress at the same rate, so with a few long
 // units per slot the last units end far apart (measured on 256^2 pixels x 256 chirps
@@ -156,6 +162,7 @@ struct FocusUnit {
 // Kernel-side status bits (written to the status word in scratch).
 enum StatusBits : int {
     kStatusTimeout = 1,
+    kStatusBadJob = 2,  // a kernel found a job record outside what it takes (no work done for it)
 };
 
 // ---- launchers (defined in the .cu files) ----
@@ -179,9 +186,12 @@ cudaError_t launch_focus_fp32_seg(const FocusJob *jobs_dev, const FocusUnit *uni
 int focus_fp32_seg_blocks_per_sm(int stage_bytes);
 // skip_zero: skip chirps whose window is zero for a whole warp (any job with a finite band).
 // store_sums: also write job.chirp_sums (whole-row staging only).
+// anchored: anchored ranges (neither skip_zero nor store_sums; flat tiles; at most
+// kAnchorMaxStageChirps chirps a stage; every pixel within kAnchorMaxDistance of its anchor).
 cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_dev, int n_units,
                               int *counter_dev, int *status_dev, int stage_bytes, int grid_ctas,
-                              bool skip_zero, bool store_sums, cudaStream_t st);
+                              bool skip_zero, bool store_sums, bool anchored, cudaStream_t st);
+int focus_fp32_anchor_blocks_per_sm(int stage_bytes);
 // Smooth-motion focus (tdc_motion.cu): per-sample positions given by job.chirps as
 // MotionRec records, rows staged whole (stage_bytes >= chirps x (s_pad x 8 + 80)),
 // psi linearised over segments of job.seg_len samples (a power of two >= 8).
@@ -241,6 +251,6 @@ inline int set_last_error(int code, const std::string &msg) { return set_last_er
 
 // Occupancy of the FP32-bulk kernel at a given dynamic shared memory size.
 int focus_fp32_blocks_per_sm(int stage_bytes);
-int focus_fp32_smem_bytes(int stage_bytes);
+int focus_fp32_smem_bytes(int stage_bytes, bool anchored = false);
 
 }  // namespace tdc

@@ -71,16 +71,6 @@ __device__ __forceinline__ float2 horner_block(float2 h, float2 ql, const float2
     return make_float2(tr, ti);
 }
 
-// (cos t, sin t) for |t| <= 0.8 by their Taylor series to t^8 / t^9 (error < 3e-8).
-__device__ __forceinline__ float2 sincos_small(float t)
-{
-    const float t2 = t * t;
-    const float c = fmaf(-0.5f * t2, fmaf(-t2 * (1.0f / 12.0f), fmaf(-t2, 1.0f / 30.0f, 1.0f), 1.0f), 1.0f);
-    const float s = t * fmaf(-t2 * (1.0f / 6.0f), fmaf(-t2 * (1.0f / 20.0f), fmaf(-t2, 1.0f / 42.0f, 1.0f), 1.0f),
-                             1.0f);
-    return make_float2(c, s);
-}
-
 // Per-(pixel, chirp) coefficients of psi: N(s) = s (n1 + s (n2 + s (k3 + s k4))), the
 // range change d = (N ia) f(N ib), ia = 1/(2 R0), ib = 1/R0^2, and g_s = g0 + g1 s.
 struct PsiCoef {

@@ -214,7 +214,7 @@ int enqueue(const tdc_noalloc_focus_args *a, float *image_dev, cudaStream_t st, 
     e = launch_focus_fp32(reinterpret_cast<const FocusJob *>(base + kOffJob),
                           reinterpret_cast<const FocusUnit *>(base + kOffUnits), (int)n_units,
                           reinterpret_cast<int *>(base + kOffStatus), reinterpret_cast<int *>(base + kOffStatus) + 1,
-                          stage_bytes, grid, std::isfinite(job.half_bw), false, st);
+                          stage_bytes, grid, std::isfinite(job.half_bw), false, false, st);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("focus kernel: ") + cudaGetErrorString(e));
     e = launch_focus_reduce(job.partial, n_groups, P, reinterpret_cast<float2 *>(image_dev), st);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("reduce kernel: ") + cudaGetErrorString(e));
@@ -235,6 +235,7 @@ extern "C" int tdc_focus_noalloc(const tdc_noalloc_focus_args *a, float *image_d
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(TDC_ERR_CUDA, std::string("focus: ") + cudaGetErrorString(e));
     if (status & kStatusTimeout) return fail(TDC_ERR_TIMEOUT, "focus kernel wait timed out");
+    if (status & kStatusBadJob) return fail(TDC_ERR_CUDA, "focus kernel rejected its job record");
     return TDC_OK;
 }
 

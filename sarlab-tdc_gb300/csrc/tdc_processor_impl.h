@@ -184,6 +184,12 @@ struct tdc_processor {
     bool grid_lo_valid = false;
     double grid_min[3] = {0, 0, 0}, grid_max[3] = {0, 0, 0};
     double axis_c[3] = {0, 0, 0}, axis_r[3] = {0, 0, 0};  // grid column / row steps (first pixel's)
+    // Anchored ranges of the FP32-bulk kernel: the largest distance of a pixel from the anchor
+    // of its group of 32 consecutive pixels (the group's 17th pixel, or its last); the kernel
+    // takes them when this is within kAnchorMaxDistance, unless switched off.
+    double anchor_span = 0.0;
+    bool anchor_enabled = true;
+    bool rec_finite = false;  // every chirp record's velocity and window centre is finite
     double vel_dir[3] = {0, 0, 0};                         // mean antenna velocity direction (0: at rest)
     tdc::impl::DevBuf grid_stage, grid_hi, grid_lo;
     // Centre pixel (x, y, z) of each work tile, flat tiles and block tiles.
@@ -235,6 +241,7 @@ struct FocusPlan {
     int cb = 1;           // chirps per pipeline stage
     int stage_bytes = 0;  // bytes per pipeline stage
     int slots = 0;        // resident CTAs of the kernel on the device
+    bool anchored = false;  // FP32-bulk kernel with anchored ranges
     size_t off_job = 0;   // job record and unit table offsets in the processor's scratch
     size_t off_units = 0;
     FocusJob job{};       // partial -> the processor's scratch

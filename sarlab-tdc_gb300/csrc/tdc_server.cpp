@@ -239,11 +239,12 @@ void tdc_server::collect(std::vector<Job *> &finished)
         if (!b.in_flight || cudaEventQuery(b.ev) != cudaSuccess) continue;
         b.in_flight = false;
         const int status = reinterpret_cast<int *>(b.host.p)[1];
-        if (status & kStatusTimeout) {
+        if (status & (kStatusTimeout | kStatusBadJob)) {
             for (Job *j : b.members)
                 if (j->state == kActive || j->state == kCompleting) {
-                    j->rc = TDC_ERR_TIMEOUT;
-                    j->err = "focus kernel wait timed out";
+                    j->rc = (status & kStatusTimeout) ? TDC_ERR_TIMEOUT : TDC_ERR_CUDA;
+                    j->err = (status & kStatusTimeout) ? "focus kernel wait timed out"
+                                                       : "focus kernel rejected its job record";
                 }
         }
     }
@@ -305,6 +306,12 @@ void tdc_server::launch_batch()
         const double t = now_ms() - t0;
         std::stable_sort(members.begin(), members.end(),
                          [&](Job *a, Job *b) { return score(a, t) < score(b, t); });
+        // A launch takes jobs of one kind only, anchored ranges or not (the first job's), so
+        // that a job's arithmetic does not depend on the jobs it shares a launch with.
+        const bool anchored = members[0]->plan.anchored;
+        members.erase(std::remove_if(members.begin(), members.end(),
+                                     [&](Job *j) { return j->plan.anchored != anchored; }),
+                      members.end());
         if ((int)members.size() > kMaxBatchJobs) members.resize(kMaxBatchJobs);
     }
     const size_t min_units = (size_t)std::max(1, 2 * n_sm * 3);
@@ -342,6 +349,7 @@ void tdc_server::launch_batch()
     FocusUnit *hu = reinterpret_cast<FocusUnit *>(h + off_units);
     int stage_bytes = 0;
     bool skip_zero = false;  // any job with a finite Doppler band
+    bool anchored = true;    // every job planned for anchored ranges
     b.finishing.clear();
     b.members = members;
     const double t = now_ms() - t0;
@@ -365,18 +373,21 @@ void tdc_server::launch_batch()
         hj[i] = j->plan.job;
         stage_bytes = std::max(stage_bytes, j->plan.stage_bytes);
         skip_zero = skip_zero || std::isfinite(j->plan.job.half_bw);
+        anchored = anchored && j->plan.anchored;
         j->next_unit += take[i];
         if (j->t_first < 0) j->t_first = t;
         if (j->next_unit == j->n_units) b.finishing.push_back(j);
     }
     int err = 0;
     err |= cudaMemcpyAsync(b.dev.p, b.host.p, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess;
-    const int bps = focus_fp32_blocks_per_sm(stage_bytes);
+    anchored = anchored && !skip_zero;
+    const int bps = anchored ? focus_fp32_anchor_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
     const int grid = (int)std::min<size_t>(n_units, (size_t)std::max(1, n_sm * bps));
     unsigned char *d = static_cast<unsigned char *>(b.dev.p);
     err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
                              reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
-                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, false, st) != cudaSuccess;
+                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, false, anchored,
+                             st) != cudaSuccess;
     err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess;
     stats.launches++;
     if (!b.finishing.empty() && batches[bi ^ 1].in_flight) {

@@ -9,37 +9,51 @@ with no collective on the data path: the gather moves only the finished image (8
 pixel).
 
 Each rank plans its chirp groups for the whole grid's pixel count
-(``TdcProcessor.setPlanPixels``). A pixel's summation order depends only on those groups,
-so on GPUs of one kind the gathered image equals a single-GPU focus of the whole grid bit
-for bit.
+(``TdcProcessor.setPlanPixels``), and every block starts on a multiple of 32 pixels (the
+engine's anchored ranges share an anchor among up to 32 consecutive pixels of a grid). A
+pixel's arithmetic then depends only on the chirp groups and its own group of 32 pixels, so
+on GPUs of one kind the gathered image equals a single-GPU focus of the whole grid bit for
+bit.
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
 
-def row_blocks(n_rows: int, world_size: int) -> list[tuple[int, int]]:
-    """Contiguous [r0, r1) row blocks of a grid with n_rows rows, one per rank, sizes differing
-    by at most one row (the first n_rows % world_size blocks are the longer ones; with fewer
-    rows than ranks the last blocks are empty)."""
+def row_align(n_cols: int) -> int:
+    """Rows per block step for a grid of n_cols columns: the fewest rows that hold a multiple
+    of 32 pixels (1 when n_cols is a multiple of 32)."""
+    return 32 // math.gcd(max(int(n_cols), 1), 32)
+
+
+def row_blocks(n_rows: int, world_size: int, align: int = 1) -> list[tuple[int, int]]:
+    """Contiguous [r0, r1) row blocks of a grid with n_rows rows, one per rank, each starting on
+    a multiple of ``align`` rows: steps of ``align`` rows are shared out, the first
+    (steps % world_size) blocks taking one step more, and the last non-empty block ends at
+    n_rows (with fewer steps than ranks the last blocks are empty)."""
     if world_size < 1:
         raise ValueError("world_size must be at least 1")
     if n_rows < 0:
         raise ValueError("n_rows must not be negative")
-    base, extra = divmod(n_rows, world_size)
-    out, r0 = [], 0
+    if align < 1:
+        raise ValueError("align must be at least 1")
+    steps = -(-n_rows // align)
+    base, extra = divmod(steps, world_size)
+    out, s0 = [], 0
     for k in range(world_size):
-        r1 = r0 + base + (1 if k < extra else 0)
-        out.append((r0, r1))
-        r0 = r1
+        s1 = s0 + base + (1 if k < extra else 0)
+        out.append((min(s0 * align, n_rows), min(s1 * align, n_rows)))
+        s0 = s1
     return out
 
 
-def rank_rows(n_rows: int, world_size: int, rank: int) -> tuple[int, int]:
+def rank_rows(n_rows: int, world_size: int, rank: int, align: int = 1) -> tuple[int, int]:
     """The [r0, r1) row block of one rank."""
     if not 0 <= rank < world_size:
         raise ValueError(f"rank {rank} outside 0..{world_size - 1}")
-    return row_blocks(n_rows, world_size)[rank]
+    return row_blocks(n_rows, world_size, align)[rank]
 
 
 def gather_rows(local: np.ndarray, n_rows: int, n_cols: int, group=None) -> np.ndarray:
@@ -51,7 +65,7 @@ def gather_rows(local: np.ndarray, n_rows: int, n_cols: int, group=None) -> np.n
     import torch.distributed as dist
 
     world = dist.get_world_size(group)
-    blocks = row_blocks(n_rows, world)
+    blocks = row_blocks(n_rows, world, row_align(n_cols))
     rmax = max(r1 - r0 for r0, r1 in blocks)
     local = np.ascontiguousarray(local, dtype=np.complex64).reshape(-1, n_cols)
     rank = dist.get_rank(group)
@@ -103,7 +117,7 @@ class ShardedProcessor:
         if g.ndim != 3 or g.shape[2] != 3:
             raise RuntimeError("focusGrid shape is incorrect")
         n_rows, n_cols = g.shape[:2]
-        r0, r1 = rank_rows(n_rows, self.world_size, self.rank)
+        r0, r1 = rank_rows(n_rows, self.world_size, self.rank, row_align(n_cols))
         self.rows = (r0, r1)
         self.shape = (n_rows, n_cols)
         setter(np.ascontiguousarray(g[r0:r1]))

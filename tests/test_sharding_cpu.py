@@ -34,6 +34,26 @@ def test_row_blocks_cover_the_grid_in_order():
         sharding.rank_rows(4, 2, 2)
 
 
+def test_row_blocks_start_on_multiples_of_32_pixels():
+    """Blocks start on whole steps of row_align(n_cols) rows, so every block's first pixel is a
+    multiple of 32 (the engine's anchor groups are the same in a block as in the whole grid)."""
+    assert [sharding.row_align(c) for c in (1024, 96, 16, 9, 48, 1)] == [1, 1, 2, 32, 2, 32]
+    for n_rows in (0, 1, 5, 13, 100, 1023):
+        for n_cols in (9, 16, 48, 100, 256):
+            a = sharding.row_align(n_cols)
+            for world in (1, 2, 3, 5):
+                blocks = sharding.row_blocks(n_rows, world, a)
+                assert blocks[0][0] == 0 and max(r1 for _, r1 in blocks) == n_rows
+                assert all(blocks[k][1] == blocks[k + 1][0] for k in range(world - 1))
+                for r0, r1 in blocks:
+                    assert r0 <= r1 and (r0 * n_cols) % 32 == 0 or r0 == n_rows
+                sizes = [r1 - r0 for r0, r1 in blocks]
+                assert max(sizes) - min(sizes) <= 2 * a - 1  # (the last block ends at n_rows)
+    assert sharding.row_blocks(13, 2, 2) == [(0, 8), (8, 13)]
+    with pytest.raises(ValueError):
+        sharding.row_blocks(4, 2, 0)
+
+
 class OracleProcessor:
     """The processor interface with the FP64 oracle computing the focus (a CPU stand-in for
     the GPU engine, test infrastructure only)."""
@@ -64,7 +84,7 @@ class OracleProcessor:
 
 
 def _scene():
-    sc = scenes.small_scene(seed=17, n_pri=96, n_samples=48, nx=9, ny=13, jitter=0.2e-3)
+    sc = scenes.small_scene(seed=17, n_pri=96, n_samples=48, nx=16, ny=13, jitter=0.2e-3)
     return sc, sc.api_arrays()
 
 
@@ -97,7 +117,8 @@ def _rank_main(rank, world, port, out_dir):
 
 @pytest.mark.parametrize("world", [2, 3])
 def test_ranks_gather_the_single_rank_image(tmp_path, world):
-    """world_size 2 (13 rows: blocks of 7 and 6) and 3 over gloo, one process per rank."""
+    """world_size 2 (13 rows of 16 pixels: blocks of 8 and 5 rows) and 3 over gloo, one process
+    per rank."""
     import torch.multiprocessing as mp
 
     mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
@@ -107,7 +128,7 @@ def test_ranks_gather_the_single_rank_image(tmp_path, world):
     single.setFocusGrid(sc.grid)
     single.start(*START)
     full = single.getFocusedImage()
-    blocks = sharding.row_blocks(full.shape[0], world)
+    blocks = sharding.row_blocks(full.shape[0], world, sharding.row_align(full.shape[1]))
     for rank in range(world):
         np.testing.assert_array_equal(np.load(tmp_path / f"image{rank}.npy"), full)
         r0, r1 = blocks[rank]
