@@ -1043,10 +1043,10 @@ int sample_records(tdc_processor *p)
 // Anchored ranges for an FP32-bulk focus staged whole, cb chirps a stage: the plain kernel
 // instance (unbounded band, so flat tiles; no kept per-chirp sums) with finite velocities and
 // window centres (the instance then forms no Doppler window), 3 to kAnchorMaxStageChirps
-// chirps a stage (with fewer, a pass of the warp's lanes over a stage's anchor records costs
-// about what the pixels save: S = 1024 measured 0.4% slower), every pixel within
-// kAnchorMaxDistance of its anchor, and the block step's correction 2 pi L g1 |dR| within its
-// series' range (0.8 rad).
+// chirps a stage (with 1 or 2, i.e. rows of about 1,000 samples or more, the instance measured
+// 0.4-1.8% slower than the double-float one: the Horner loop dominates there), every pixel
+// within kAnchorMaxDistance of its anchor, and the block step's correction 2 pi L g1 |dR|
+// within its series' range (0.25 rad: rows of 256 samples at 2 mm spacing, 128 at 1 mm).
 bool anchor_eligible(const tdc_processor *p, int cb)
 {
     if (!p->anchor_enabled || p->keep_sums || !p->per_chirp || !p->rec_finite) return false;
@@ -1054,7 +1054,7 @@ bool anchor_eligible(const tdc_processor *p, int cb)
     if (cb < 3 || cb > kAnchorMaxStageChirps) return false;
     if (!(p->anchor_span <= kAnchorMaxDistance)) return false;
     const double g1 = 2.0 * p->F1 / kC0;
-    return 2.0 * M_PI * 8.0 * std::fabs(g1) * p->anchor_span <= 0.8;
+    return 2.0 * M_PI * 8.0 * std::fabs(g1) * p->anchor_span <= 0.25;
 }
 
 int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)

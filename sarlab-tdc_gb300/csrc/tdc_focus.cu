@@ -66,7 +66,8 @@ struct SharedPixel {
 // 4 slots x chirps anchor records take one or two passes of the warp's lanes); a pixel then
 // needs only its range difference dR = R - R0 = d.(d - 2e) / (R0 + R) in FP32 (d = pixel -
 // anchor, e = antenna - anchor: no cancellation, |dR| <= |d|) and small corrections
-// alpha0 + g0 dR, beta0 + g1 dR, QL0 e^{j 2 pi L g1 dR}. With an unbounded band and finite
+// alpha0 + g0 dR, beta0 + g1 dR, QL0 e^{j 2 pi L g1 dR} (|2 pi L g1 dR| <= 0.25 by the host's
+// bound). With an unbounded band and finite
 // velocities and window centres, a chirp's window weight is 1 (0 where the antenna sits on the
 // pixel: NaN Doppler), so this instance forms no Doppler frequency. Its chirp sums q0 H go
 // into a per-stage sum by complex FMA, and the stage sums into the Kahan-compensated sum.
@@ -76,6 +77,16 @@ struct SharedAnchor {
     float anc[kFocusThreads / 32][kFocusPT][6];      // anchor per (warp, slot): hi xyz, lo xyz
     float4 rec[kFocusThreads / 32][kAnchorRecs][2];  // per (chirp, slot): (e, R0), (alpha0, beta0, QL0)
 };
+
+// (cos t, sin t) for |t| <= 0.25 (the anchored block-step correction, host-bounded) by their
+// Taylor series to t^6 / t^5 (error < 2e-8).
+__device__ __forceinline__ float2 sincos_anchor(float t)
+{
+    const float t2 = t * t;
+    const float c = fmaf(t2, fmaf(t2, fmaf(t2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
+    const float s = t * fmaf(t2, fmaf(t2, 1.0f / 120.0f, -1.0f / 6.0f), 1.0f);
+    return make_float2(c, s);
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -162,6 +173,31 @@ __device__ __forceinline__ void chirp_phasors(float rh, float rl, float g0h, flo
     float sa, ca;
     __sincosf(kTwoPiF * alpha, &sa, &ca);
     q0 = make_float2(w * ca, w * sa);
+}
+
+// Anchor record of one (chirp, anchor): e = antenna - anchor, R0 (both rounded to FP32),
+// alpha0 = frac(g0 R0), beta0 = frac(g1 R0) and QL0 = e^{j 2 pi L beta0}, from double-float R0.
+__device__ __forceinline__ void anchor_record(const ChirpRec &r, const float *A, float g0h, float g0l, float g1,
+                                              float g1l, float4 &rec0, float4 &rec1)
+{
+    float exh, exl, eyh, eyl, ezh, ezl;
+    dd_sub(r.p_hi.x, r.p_lo.x, A[0], A[3], exh, exl);
+    dd_sub(r.p_hi.y, r.p_lo.y, A[1], A[4], eyh, eyl);
+    dd_sub(r.p_hi.z, r.p_lo.z, A[2], A[5], ezh, ezl);
+    float rh, rl, rs, dh;
+    dd_range(exh, exl, eyh, eyl, ezh, ezl, rh, rl, rs, dh);
+    const float alpha0 = dd_frac_mul(g0h, g0l, rh, rl);
+    float bh = g1 * rh;
+    float bl = fmaf(g1, rh, -bh);
+    bl = fmaf(g1, rl, bl);
+    bl = fmaf(g1l, rh, bl);
+    bh -= rintf(bh);
+    const float lbh = (float)kL * bh;  // exact
+    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
+    float sl, cl;
+    sincospif(2.0f * lfr, &sl, &cl);
+    rec0 = make_float4(exh + exl, eyh + eyl, ezh + ezl, rh + rl);
+    rec1 = make_float4(alpha0, bh + bl, cl, sl);
 }
 
 // Pixel of a unit's slot (valid when unit_pixel_ok). Block tiles come with a finite band,
@@ -365,31 +401,14 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
             for (int i = 0; i < kFocusPT; ++i) ssum[i] = make_float2(0.f, 0.f);
 
             if constexpr (ANCHOR) {
-                // The stage's anchor records, record k = chirp x 4 + slot, from the staged chirp
-                // records (forming them for several stages at a time from the records in global
-                // memory measured 2-3.5% slower: every warp of the CTA waits on those loads).
-                for (int k = lane; k < kFocusPT * cnt; k += 32) {
-                    const ChirpRec r = recs[k >> 2];
-                    const float *A = sa.anc[warp][k & (kFocusPT - 1)];
-                    float exh, exl, eyh, eyl, ezh, ezl;
-                    dd_sub(r.p_hi.x, r.p_lo.x, A[0], A[3], exh, exl);
-                    dd_sub(r.p_hi.y, r.p_lo.y, A[1], A[4], eyh, eyl);
-                    dd_sub(r.p_hi.z, r.p_lo.z, A[2], A[5], ezh, ezl);
-                    float rh, rl, rs, dh;
-                    dd_range(exh, exl, eyh, eyl, ezh, ezl, rh, rl, rs, dh);
-                    const float alpha0 = dd_frac_mul(g0h, g0l, rh, rl);
-                    float bh = g1 * rh;
-                    float bl = fmaf(g1, rh, -bh);
-                    bl = fmaf(g1, rl, bl);
-                    bl = fmaf(g1l, rh, bl);
-                    bh -= rintf(bh);
-                    const float lbh = (float)kL * bh;  // exact
-                    const float lfr = (lbh - rintf(lbh)) + (float)kL * bl;
-                    float sl, cl;
-                    sincospif(2.0f * lfr, &sl, &cl);
-                    sa.rec[warp][k][0] = make_float4(exh + exl, eyh + eyl, ezh + ezl, rh + rl);
-                    sa.rec[warp][k][1] = make_float4(alpha0, bh + bl, cl, sl);
-                }
+                // The stage's anchor records for this warp, record k = chirp x 4 + slot, from the
+                // staged chirp records. (Forming several stages' records at a time from the
+                // records in global memory measured 2-3.5% slower, every warp of the CTA waiting
+                // on those loads; one warp in turn forming the whole CTA's a stage ahead did not
+                // make rows of 1-2 chirps a stage pay either.)
+                for (int k = lane; k < kFocusPT * cnt; k += 32)
+                    anchor_record(recs[k >> 2], sa.anc[warp][k & (kFocusPT - 1)], g0h, g0l, g1, g1l,
+                                  sa.rec[warp][k][0], sa.rec[warp][k][1]);
                 __syncwarp();
             }
 
@@ -441,12 +460,11 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                         const float den = e.w + rr;
                         const float dr = den > 0.0f ? __fdividef(num, den) : 0.0f;
                         const float w = r2 > 0.0f ? wskip[i] : 0.0f;
-                        // start phase alpha0 + g0 dR modulo one cycle (te: the product's rounding and g0's
-                        // low part)
-                        const float t = g0h * dr;
-                        const float te = fmaf(g0l, dr, fmaf(g0h, dr, -t));
-                        float a = (t - rintf(t)) + a1.x;
-                        a = (a - rintf(a)) + te;
+                        // start phase alpha0 + g0 dR modulo one cycle: g0h dR less its nearest integer
+                        // in one rounding (|.| <= 1/2), then alpha0 and g0's low part
+                        float a = fmaf(g0h, dr, -rintf(g0h * dr)) + a1.x;
+                        a = fmaf(g0l, dr, a);
+                        a -= rintf(a);
                         float sa0, ca0;
                         __sincosf(kTwoPiF * a, &sa0, &ca0);
                         q0[i] = make_float2(w * ca0, w * sa0);
@@ -455,7 +473,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                         p[i][0] = make_float2(c1s, s1);
 #pragma unroll
                         for (int q = 1; q < kL - 1; ++q) p[i][q] = cmul(p[i][q - 1], p[i][0]);
-                        ql[i] = cmul(make_float2(a1.z, a1.w), sincos_small(kql * dr));
+                        ql[i] = cmul(make_float2(a1.z, a1.w), sincos_anchor(kql * dr));
                         h[i] = make_float2(0.f, 0.f);
                     }
                 } else if (SKIP_ZERO && kEarlyVote) {

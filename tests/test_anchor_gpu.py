@@ -56,12 +56,11 @@ def _compare(api, grid, group, pos64=None, grid64=False):
 @pytest.mark.parametrize("n_samples,group", [(128, 32), (256, 32), (512, 32), (640, 32), (1024, 0), (2048, 0)])
 def test_anchor_groups_against_oracle(cuda_device, n_samples, group):
     """Rows staged 15, 7, 4 and 3 chirps a stage (one or two passes of anchor records), and none
-    at 1 or 2 chirps a stage, where a pass over a stage's anchor records costs about what the
-    pixels save; on a 19 x 57 grid: rows of 19 pixels
-    (3.8 cm), so groups wrap rows and stay within the 5 cm bound, and 1,083 pixels end in a
-    partial tile and a partial group."""
+    at 1 or 2 chirps a stage, where the double-float instance is faster; on a 19 x 57 grid at
+    1 mm: rows of 19 pixels (1.9 cm), so groups wrap rows and stay within the anchor bounds, and
+    1,083 pixels end in a partial tile and a partial group."""
     sc = scenes.small_scene(seed=40 + n_samples, n_pri=96, n_samples=n_samples, nx=19, ny=57, jitter=0.3e-3,
-                            device="cuda")
+                            spacing=1e-3, device="cuda")
     _compare(sc.api_arrays(), sc.grid.astype(np.float32), group)
 
 
