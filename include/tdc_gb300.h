@@ -334,6 +334,7 @@ typedef struct tdc_server_stats {
     int64_t device_bytes_in_use;
     int queued;
     int active;
+    int64_t unbatched;    /* jobs focused alone beside the launches (the FP64 general path) */
 } tdc_server_stats;
 
 /* memory_budget_bytes = 0: half of the free device memory; max_jobs = 0: 32 (at most 64). */

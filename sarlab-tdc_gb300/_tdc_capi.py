@@ -101,6 +101,7 @@ class ServerStats(C.Structure):
         ("device_bytes_in_use", C.c_int64),
         ("queued", C.c_int),
         ("active", C.c_int),
+        ("unbatched", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -66,7 +66,7 @@ struct Job {
     FocusPlan plan;
     size_t next_unit = 0;
     size_t n_units = 0;
-    double unit_work = 0;  // correlations per unit
+    double unit_work = 0;  // correlations per unit, in FP32-bulk kernel time (kind_cost)
     size_t footprint = 0;
     int state = kQueued;
     int rc = TDC_OK;
@@ -94,6 +94,23 @@ constexpr double kServerBatchWork = 1.0e12;
 // are not starved (a job gains kAging seconds of priority per second it waits).
 constexpr double kRateEstimate = 7.0e12;  // correlations per second
 constexpr double kAging = 0.5;
+
+// The kernel a job's units run in: jobs share a launch only with jobs of the same kind (the
+// same kernel instance, so a job's arithmetic does not depend on the jobs beside it). -1: not
+// batched (the FP64 general path: focused alone on the side stream).
+int job_kind(const FocusPlan &pl)
+{
+    if (pl.path == TDC_PATH_FP32_BULK) return pl.seg ? 1 : (pl.anchored ? 2 : 0);
+    if (pl.path == TDC_PATH_GENERAL) return 16 + pl.variant;
+    return -1;
+}
+
+// Time of a correlation on a job's kernel relative to the FP32-bulk kernel's (GB300): a
+// launch's work budget and the scheduling priority count in FP32-bulk correlations.
+double kind_cost(int kind)
+{
+    return kind >= 16 ? ((kind - 16) & 2 ? 9.0 : 5.5) : 1.0;
+}
 
 size_t device_footprint(const tdc_job_desc &d, int n_sm)
 {
@@ -146,7 +163,7 @@ struct tdc_server {
     // Launches alternate between two streams, so the next launch's CTAs take the
     // SMs that the previous launch's last units leave idle.
     cudaStream_t compute[2] = {nullptr, nullptr};
-    cudaStream_t side = nullptr;  // unbatched jobs (FP64 / general paths), launch priority
+    cudaStream_t side = nullptr;  // unbatched jobs (FP64 general path), launch priority
     Batch batches[2];
     int next_batch = 0;
     tdc_server_stats stats{};
@@ -227,7 +244,7 @@ int tdc_server::admit_one(Job *j)
     if (cudaStreamSynchronize(p->stream) != cudaSuccess) return set_last_error(TDC_ERR_CUDA, "slot stream sync");
     j->n_units = p->units_host.size();
     j->next_unit = 0;
-    j->unit_work = (double)kFocusTile * j->plan.job.chirps_per_group * d.n_samples;
+    j->unit_work = (double)kFocusTile * j->plan.job.chirps_per_group * d.n_samples * kind_cost(job_kind(j->plan));
     return TDC_OK;
 }
 
@@ -306,11 +323,11 @@ void tdc_server::launch_batch()
         const double t = now_ms() - t0;
         std::stable_sort(members.begin(), members.end(),
                          [&](Job *a, Job *b) { return score(a, t) < score(b, t); });
-        // A launch takes jobs of one kind only, anchored ranges or not (the first job's), so
-        // that a job's arithmetic does not depend on the jobs it shares a launch with.
-        const bool anchored = members[0]->plan.anchored;
+        // A launch takes jobs of one kind only (the first job's: job_kind), so that a job's
+        // arithmetic does not depend on the jobs it shares a launch with.
+        const int kind = job_kind(members[0]->plan);
         members.erase(std::remove_if(members.begin(), members.end(),
-                                     [&](Job *j) { return j->plan.anchored != anchored; }),
+                                     [&](Job *j) { return job_kind(j->plan) != kind; }),
                       members.end());
         if ((int)members.size() > kMaxBatchJobs) members.resize(kMaxBatchJobs);
     }
@@ -381,13 +398,28 @@ void tdc_server::launch_batch()
     int err = 0;
     err |= cudaMemcpyAsync(b.dev.p, b.host.p, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess;
     anchored = anchored && !skip_zero;
-    const int bps = anchored ? focus_fp32_anchor_blocks_per_sm(stage_bytes) : focus_fp32_blocks_per_sm(stage_bytes);
+    const int kind = job_kind(members[0]->plan);
+    const bool seg = kind == 1;
+    const bool general = kind >= 16;
+    const int variant = general ? members[0]->plan.variant : 0;
+    const int bps = general    ? focus_general_blocks_per_sm(variant, stage_bytes)
+                    : seg      ? focus_fp32_seg_blocks_per_sm(stage_bytes)
+                    : anchored ? focus_fp32_anchor_blocks_per_sm(stage_bytes)
+                               : focus_fp32_blocks_per_sm(stage_bytes);
     const int grid = (int)std::min<size_t>(n_units, (size_t)std::max(1, n_sm * bps));
     unsigned char *d = static_cast<unsigned char *>(b.dev.p);
-    err |= launch_focus_fp32(reinterpret_cast<const FocusJob *>(d + kBatchOffJobs),
-                             reinterpret_cast<const FocusUnit *>(d + off_units), (int)n_units, reinterpret_cast<int *>(d),
-                             reinterpret_cast<int *>(d) + 1, stage_bytes, grid, skip_zero, false, anchored,
-                             st) != cudaSuccess;
+    const FocusJob *jobs_d = reinterpret_cast<const FocusJob *>(d + kBatchOffJobs);
+    const FocusUnit *units_d = reinterpret_cast<const FocusUnit *>(d + off_units);
+    int *counter_d = reinterpret_cast<int *>(d);
+    if (general)
+        err |= launch_focus_general(variant, jobs_d, units_d, (int)n_units, counter_d, counter_d + 1, stage_bytes, grid,
+                                    st) != cudaSuccess;
+    else if (seg)
+        err |= launch_focus_fp32_seg(jobs_d, units_d, (int)n_units, counter_d, counter_d + 1, stage_bytes, grid,
+                                     skip_zero, st) != cudaSuccess;
+    else
+        err |= launch_focus_fp32(jobs_d, units_d, (int)n_units, counter_d, counter_d + 1, stage_bytes, grid, skip_zero,
+                                 false, anchored, st) != cudaSuccess;
     err |= cudaMemcpyAsync(b.host.p, b.dev.p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess;
     stats.launches++;
     if (!b.finishing.empty() && batches[bi ^ 1].in_flight) {
@@ -478,12 +510,15 @@ void tdc_server::admit_loop()
         const int rc = admit_one(j);
         int rc2 = TDC_OK;
         std::string err2;
-        const bool batched = j->plan.path == TDC_PATH_FP32_BULK && !j->plan.seg;
+        const bool batched = job_kind(j->plan) >= 0;
         if (!rc && !batched) {
-            // FP64 / general path or rows staged in segments: not batched, focused on its own
-            // on the side stream (at the launch streams' priority, so it shares the SMs with
-            // the batches).
+            // FP64 general path: not batched, focused on its own on the side stream (at the
+            // launch streams' priority, so it shares the SMs with the batches).
             tdc_processor *p = j->slot;
+            {
+                std::lock_guard<std::mutex> g(mu);
+                stats.unbatched++;
+            }
             rc2 = tdc_processor_focus_device(p, p->image_dev.as<float>(), side);
             if (rc2) {
                 err2 = tdc_last_error();

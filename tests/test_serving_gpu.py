@@ -108,34 +108,57 @@ def test_job_over_budget_fails_alone(cuda_device):
         assert info["status"] == 0
 
 
-def test_unbatched_general_path_job_in_a_mix(cuda_device):
-    """A job the FP32-bulk kernel cannot take (jittered sample times: FP32 general kernel) runs
-    unbatched beside batched jobs and gives the processor's image bit for bit."""
+def _jittered_times(sc, seed):
+    st = sc.radar.sample_times().astype(np.float64)
+    st += np.random.default_rng(seed).uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
+    return st.astype(np.float32)
+
+
+def _processor_image(sc, sample_times=None):
     import _sarlabtdc
+
+    p = _sarlabtdc.TdcProcessor(0)
+    api = sc.api_arrays()
+    if sample_times is not None:
+        api["sampleTimes"] = sample_times
+    p.setRawData(*api.values())
+    p.setChirpPositionsF64(sc.positions)
+    p.setFocusGridF64(sc.grid)
+    p.start(*START)
+    return p.getFocusedImage().ravel(), p.lastStats()
+
+
+def test_general_and_long_row_jobs_are_batched_by_kind(cuda_device):
+    """Jobs the FP32-bulk kernel cannot take whole (jittered sample times: the FP32 general
+    kernel; rows too long for the stages: the segmented kernel) are batched with jobs of their
+    own kind, beside the bulk launches, and each gives the processor's image bit for bit."""
     from sarlabtdc.serving import FocusServer
 
-    jobs = _jobs()[:3]
-    odd = scenes.small_scene(seed=13, n_pri=300, n_samples=96, nx=40, ny=30, jitter=0.2e-3, device="cuda")
-    st = odd.radar.sample_times().astype(np.float64)
-    st += np.random.default_rng(4).uniform(-0.3, 0.3, st.shape) * (st[1] - st[0])
-    st = st.astype(np.float32)
-    with FocusServer(max_jobs=4) as srv:
-        ids = [_submit(srv, sc) for sc in jobs]
-        oid = srv.submit(odd.raw, st, odd.positions, odd.grid, np.float32(odd.radar.mod_rate),
-                         np.float32(odd.radar.f0), start=START)
-        img, info = srv.wait(oid)
+    bulk = _jobs()[:2]
+    odd = [scenes.small_scene(seed=13 + k, n_pri=300, n_samples=96, nx=40, ny=30, jitter=0.2e-3, device="cuda")
+           for k in range(2)]
+    odd_t = [_jittered_times(sc, 4 + k) for k, sc in enumerate(odd)]
+    long_row = scenes.small_scene(seed=15, n_pri=48, n_samples=9600, nx=24, ny=16, jitter=0.2e-3, device="cuda")
+    with FocusServer(max_jobs=6) as srv:
+        ids = [_submit(srv, sc) for sc in bulk]
+        oids = [srv.submit(sc.raw, st, sc.positions, sc.grid, np.float32(sc.radar.mod_rate),
+                           np.float32(sc.radar.f0), start=START) for sc, st in zip(odd, odd_t)]
+        lid = _submit(srv, long_row)
+        odd_out = [srv.wait(i) for i in oids]
+        long_img, long_info = srv.wait(lid)
         for i in ids:
             assert srv.wait(i)[1]["status"] == 0
-    assert info["status"] == 0 and info["path"] == 2
-    p = _sarlabtdc.TdcProcessor(0)
-    api = odd.api_arrays()
-    api["sampleTimes"] = st
-    p.setRawData(*api.values())
-    p.setChirpPositionsF64(odd.positions)
-    p.setFocusGridF64(odd.grid)
-    p.start(*START)
-    assert p.lastStats()["path_name"] == "general"
-    np.testing.assert_array_equal(p.getFocusedImage().ravel(), img)
+        stats = srv.stats()
+    assert stats["unbatched"] == 0
+    for sc, st, (img, info) in zip(odd, odd_t, odd_out):
+        assert info["status"] == 0 and info["path"] == 2
+        ref, pst = _processor_image(sc, st)
+        assert pst["path_name"] == "general"
+        np.testing.assert_array_equal(ref, img)
+    assert long_info["status"] == 0 and long_info["path"] == 0
+    ref, pst = _processor_image(long_row)
+    assert pst["stage_chirps"] == 1 and pst["stage_samples"] < 9600
+    np.testing.assert_array_equal(ref, long_img)
 
 
 def test_finite_band_job_in_a_mix_keeps_every_image(cuda_device):
