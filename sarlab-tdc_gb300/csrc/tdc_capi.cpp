@@ -1047,11 +1047,14 @@ int sample_records(tdc_processor *p)
 // 0.4-1.8% slower than the double-float one: the Horner loop dominates there), every pixel
 // within kAnchorMaxDistance of its anchor, and the block step's correction 2 pi L g1 |dR|
 // within its series' range (0.25 rad: rows of 256 samples at 2 mm spacing, 128 at 1 mm).
+#ifndef TDC_ANCHOR_MIN_STAGE_CHIRPS
+#define TDC_ANCHOR_MIN_STAGE_CHIRPS 3
+#endif
 bool anchor_eligible(const tdc_processor *p, int cb)
 {
     if (!p->anchor_enabled || p->keep_sums || !p->per_chirp || !p->rec_finite) return false;
     if (std::isfinite(p->opts.bw / 2.0f)) return false;
-    if (cb < 3 || cb > kAnchorMaxStageChirps) return false;
+    if (cb < TDC_ANCHOR_MIN_STAGE_CHIRPS || cb > kAnchorMaxStageChirps) return false;
     if (!(p->anchor_span <= kAnchorMaxDistance)) return false;
     const double g1 = 2.0 * p->F1 / kC0;
     return 2.0 * M_PI * 8.0 * std::fabs(g1) * p->anchor_span <= 0.25;

@@ -54,6 +54,12 @@ constexpr int kUnrollBlocks = TDC_FOCUS_UNROLL;
 #define TDC_FOCUS_EARLY_VOTE 1
 #endif
 constexpr bool kEarlyVote = TDC_FOCUS_EARLY_VOTE != 0;
+// Anchored instance: chirp sums into a per-stage sum, the stage sums into the Kahan sum (1),
+// or every chirp sum into the Kahan sum (0).
+#ifndef TDC_ANCHOR_STAGE_SUM
+#define TDC_ANCHOR_STAGE_SUM 1
+#endif
+constexpr bool kAnchorStageSums = TDC_ANCHOR_STAGE_SUM != 0;
 
 struct SharedPixel {
     float t[kFocusPT * 6][kFocusThreads];  // (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo) per pixel slot
@@ -223,10 +229,10 @@ __device__ __forceinline__ bool unit_pixel_ok(long long p, long long P)
 // job.chirp_sums[c][p], zero for chirps skipped by the window vote (the adjoint reads them).
 // ANCHOR: anchored ranges (SharedAnchor); flat tiles and an unbounded band only, stages of at
 // most kAnchorMaxStageChirps chirps, pixels within the host's anchor distance bound.
-template <bool SKIP_ZERO, bool STORE, bool ANCHOR = false>
-__global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
-    focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
-                      int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
+template <bool SKIP_ZERO, bool STORE, bool ANCHOR>
+__device__ __forceinline__ void focus_fp32_body(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units,
+                                                int n_units, int *__restrict__ counter, int *__restrict__ status,
+                                                int stage_bytes)
 {
     static_assert(!ANCHOR || (!SKIP_ZERO && !STORE), "anchored ranges: plain instance only");
     extern __shared__ __align__(128) unsigned char smem[];
@@ -554,7 +560,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                 }
 
                 if (STORE) store_sums(c, h[0], h[1], h[2], h[3]);
-                if constexpr (ANCHOR) {
+                if constexpr (ANCHOR && kAnchorStageSums) {
 #pragma unroll
                     for (int i = 0; i < kFocusPT; ++i) {
                         ssum[i].x = fmaf(q0[i].x, h[i].x, ssum[i].x);
@@ -567,7 +573,7 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
                     for (int i = 0; i < kFocusPT; ++i) kahan_add(sum[i], comp[i], cmul(q0[i], h[i]));
                 }
             }
-            if constexpr (ANCHOR) {
+            if constexpr (ANCHOR && kAnchorStageSums) {
 #pragma unroll
                 for (int i = 0; i < kFocusPT; ++i) kahan_add(sum[i], comp[i], ssum[i]);
             }
@@ -609,6 +615,30 @@ __global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
         }
         __syncthreads();  // sJ / sp are rewritten by the next unit
     }
+}
+
+template <bool SKIP_ZERO, bool STORE>
+__global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
+    focus_fp32_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
+                      int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
+{
+    focus_fp32_body<SKIP_ZERO, STORE, false>(jobs, units, n_units, counter, status, stage_bytes);
+}
+
+// The anchored-range instance is a kernel of its own, so that its register budget can be set
+// apart from the others' (TDC_ANCHOR_MAXNREG > 0: at most that many registers a thread).
+#ifndef TDC_ANCHOR_MAXNREG
+#define TDC_ANCHOR_MAXNREG 0
+#endif
+#if TDC_ANCHOR_MAXNREG > 0
+__global__ void __maxnreg__(TDC_ANCHOR_MAXNREG)
+#else
+__global__ void __launch_bounds__(kFocusThreads, TDC_FOCUS_MINB)
+#endif
+    focus_fp32_anchored_kernel(const FocusJob *__restrict__ jobs, const FocusUnit *__restrict__ units, int n_units,
+                               int *__restrict__ counter, int *__restrict__ status, int stage_bytes)
+{
+    focus_fp32_body<false, false, true>(jobs, units, n_units, counter, status, stage_bytes);
 }
 
 // Long chirps: the same focus with a chirp's samples staged in segments of
@@ -860,8 +890,8 @@ int focus_fp32_anchor_blocks_per_sm(int stage_bytes)
 {
     const int smem = focus_fp32_smem_bytes(stage_bytes, true);
     int blocks = 0;
-    if (allow_max_dynamic_smem(focus_fp32_kernel<false, false, true>) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_kernel<false, false, true>, kFocusThreads,
+    if (allow_max_dynamic_smem(focus_fp32_anchored_kernel) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, focus_fp32_anchored_kernel, kFocusThreads,
                                                       smem) != cudaSuccess)
         return 0;
     return blocks;
@@ -889,7 +919,7 @@ cudaError_t launch_focus_fp32(const FocusJob *jobs_dev, const FocusUnit *units_d
     if (anchored && (skip_zero || store_sums)) return cudaErrorInvalidValue;
     const int smem = focus_fp32_smem_bytes(stage_bytes, anchored);
     using Fn = void (*)(const FocusJob *, const FocusUnit *, int, int *, int *, int);
-    const Fn fn = anchored    ? focus_fp32_kernel<false, false, true>
+    const Fn fn = anchored    ? focus_fp32_anchored_kernel
                   : skip_zero ? (store_sums ? focus_fp32_kernel<true, true> : focus_fp32_kernel<true, false>)
                               : (store_sums ? focus_fp32_kernel<false, true> : focus_fp32_kernel<false, false>);
     cudaError_t e = allow_max_dynamic_smem(fn);
