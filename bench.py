@@ -493,6 +493,7 @@ def run_windowed(sc, api, f64, stream, unbounded_ms, speed=0.05, band_hz=10.0, n
     return {"ms": round(ms, 2), "unbounded_ms": round(unbounded_ms, 2),
             "speedup_vs_unbounded": round(unbounded_ms / ms, 2),
             "band_hz": band_hz, "speed_m_s": speed, "tile_cols": stats["tile_cols"],
+            "span_permille": stats["span_permille"],
             "rel_l2": float(np.linalg.norm(got[pix] - ref) / np.linalg.norm(ref)), "pixels_checked": int(pix.size),
             "kernel": "focus_fp32_kernel<SKIP_ZERO>"}
 

@@ -145,7 +145,8 @@ typedef struct tdc_start_stats {
     int motion_segment;   /* smooth-motion path: samples per linearised segment; 0 on the other paths */
     int anchor_pixels;    /* FP32-bulk path with anchored ranges: consecutive pixels sharing one anchor
                              (32); 0 when every pixel's range is formed in double-float */
-    int reserved;
+    int span_permille;    /* chirps the work units visit, per mille of tiles x chirps: below 1000 when a
+                             finite Doppler band lets units skip chirps out of band for their whole tile */
 } tdc_start_stats;
 
 typedef enum tdc_path {

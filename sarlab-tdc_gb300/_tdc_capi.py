@@ -127,7 +127,7 @@ class StartStats(C.Structure):
         ("adjoint_stored", C.c_int),
         ("motion_segment", C.c_int),
         ("anchor_pixels", C.c_int),
-        ("reserved", C.c_int),
+        ("span_permille", C.c_int),
     ]
 
     def as_dict(self) -> dict:

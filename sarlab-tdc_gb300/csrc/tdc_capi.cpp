@@ -607,6 +607,7 @@ int prepare(tdc_processor *p, const StartOpts &o, int &launches)
     p->opts = o;
     p->prepared = true;
     p->xs_scaled_ready = false;
+    p->offsets_applied = false;
     ++p->state_epoch;
     p->plan_path = -1;  // job parameters changed
     return TDC_OK;
@@ -620,6 +621,7 @@ int upload_grid(tdc_processor *p, int &launches)
     const long long P = (long long)p->rows * p->cols;
     p->P = P;
     ++p->state_epoch;
+    p->plan_path = -1;  // unit spans and costs follow the grid's coordinates
     cudaStream_t st = p->stream;
     const size_t elt = p->grid64 ? 8 : 4;
     TDC_CK(p->grid_hi.ensure((size_t)P * 16), "alloc grid");
@@ -637,9 +639,17 @@ int upload_grid(tdc_processor *p, int &launches)
         if (P > 0) {
             const long long n_flat = (P + kFocusTile - 1) / kFocusTile;
             p->tile_centre_flat.resize((size_t)n_flat * 3);
+            p->tile_radius_flat.assign((size_t)n_flat, 0.0);
             for (long long t = 0; t < n_flat; ++t) {
                 const long long i = std::min(P - 1, t * kFocusTile + kFocusTile / 2);
                 for (int k = 0; k < 3; ++k) p->tile_centre_flat[3 * t + k] = g(i, k);
+                double r2 = 0.0;
+                for (long long q = t * kFocusTile; q < std::min(P, (t + 1) * kFocusTile); ++q) {
+                    const double dx = g(q, 0) - g(i, 0), dy = g(q, 1) - g(i, 1), dz = g(q, 2) - g(i, 2);
+                    const double d2 = dx * dx + dy * dy + dz * dz;
+                    r2 = d2 > r2 || d2 != d2 ? d2 : r2;
+                }
+                p->tile_radius_flat[t] = std::sqrt(r2);
             }
             // anchored ranges: distance of each pixel from its group's anchor (groups of 32
             // consecutive pixels; the anchor is the 17th pixel or the group's last)
@@ -658,11 +668,24 @@ int upload_grid(tdc_processor *p, int &launches)
             const long long n_tr = (p->rows + tile_rows - 1) / tile_rows;
             const long long n_tc = (p->cols + kBlockTileCols - 1) / kBlockTileCols;
             p->tile_centre_block.resize((size_t)(n_tr * n_tc) * 3);
+            p->tile_radius_block.assign((size_t)(n_tr * n_tc), 0.0);
             for (long long tr = 0; tr < n_tr; ++tr)
                 for (long long tc = 0; tc < n_tc; ++tc) {
                     const long long r = std::min<long long>(p->rows - 1, tr * tile_rows + tile_rows / 2);
                     const long long c = std::min<long long>(p->cols - 1, tc * kBlockTileCols + kBlockTileCols / 2);
-                    for (int k = 0; k < 3; ++k) p->tile_centre_block[3 * (tr * n_tc + tc) + k] = g(r * p->cols + c, k);
+                    const long long ci = r * p->cols + c;
+                    for (int k = 0; k < 3; ++k) p->tile_centre_block[3 * (tr * n_tc + tc) + k] = g(ci, k);
+                    double r2 = 0.0;
+                    for (long long rr = tr * tile_rows; rr < std::min<long long>(p->rows, (tr + 1) * tile_rows); ++rr)
+                        for (long long cc = tc * kBlockTileCols;
+                             cc < std::min<long long>(p->cols, (tc + 1) * kBlockTileCols); ++cc) {
+                            const long long q = rr * p->cols + cc;
+                            if (q >= P) continue;
+                            const double dx = g(q, 0) - g(ci, 0), dy = g(q, 1) - g(ci, 1), dz = g(q, 2) - g(ci, 2);
+                            const double d2 = dx * dx + dy * dy + dz * dz;
+                            r2 = d2 > r2 || d2 != d2 ? d2 : r2;
+                        }
+                    p->tile_radius_block[tr * n_tc + tc] = std::sqrt(r2);
                 }
         }
     }
@@ -839,34 +862,69 @@ int choose_tile_cols(const tdc_processor *p)
 // tile's centre pixel for each chirp of the group), so the persistent CTAs take the long
 // ones first and the launch does not end on a few long units. Only the order in which CTAs
 // take units changes: each pixel's sums, and so the image, are the same.
-void order_units_by_cost(tdc_processor *p, int tile_cols)
+// With `narrow`, each unit also gets the span of its group's chirps that any pixel of its
+// tile can see in band (FocusUnit::span), from the Doppler at the tile's centre T and a bound
+// on its change over the tile: with u(p) = (a - p) / |a - p| and |p - T| <= rho < |a - T| = n
+// (rho the tile's radius), the directions from the antenna differ by at most asin(rho / n),
+// so |u(p) - u(T)| <= 2 sin(asin(rho / n) / 2) and |fd(p) - fd(T)| <= (2 / lambda) |v| that.
+// A chirp outside the span is out of band for every pixel of the tile (with a 5% margin on
+// that bound and 1e-4 relative for the kernel's FP32 arithmetic), so the zero-window
+// instance would skip it for every warp: skipping it in the unit changes no sum.
+void order_units_by_cost(tdc_processor *p, int tile_cols, bool narrow)
 {
     if (!std::isfinite(p->opts.bw) || p->rec_host.size() != (size_t)p->C || p->units_host.size() < 2) return;
     const std::vector<double> &centres = tile_cols ? p->tile_centre_block : p->tile_centre_flat;
+    const std::vector<double> &radii = tile_cols ? p->tile_radius_block : p->tile_radius_flat;
     const long long n_tiles = (long long)centres.size() / 3;
     const int C = p->C, cpg = p->plan_cpg, groups = p->plan_groups;
     if ((long long)p->units_host.size() != n_tiles * groups) return;
-    const double two_over_lambda = 2.0 / (double)p->lambda, half_bw = 0.5 * (double)p->opts.bw;
+    narrow = narrow && (long long)radii.size() == n_tiles && cpg < (1 << 15);
+    const double two_over_lambda = (double)(2.0f / p->lambda), half_bw = (double)(p->opts.bw / 2.0f);
     std::vector<double> cost((size_t)n_tiles * groups, 0.0);
+    std::vector<int> span((size_t)n_tiles * groups, 0);
     parallel_chirps((int)n_tiles, C, [&](int, int t0, int t1) {
         for (int t = t0; t < t1; ++t) {
             const double *T = &centres[3 * (size_t)t];
+            const double rho = narrow ? radii[t] : 0.0;
             for (int g = 0; g < groups; ++g) {
                 const int c0 = g * cpg, c1 = std::min(C, c0 + cpg);
                 long live = 0;
+                int lo = c1, hi = c0;  // chirps that some pixel of the tile may see in band: [lo, hi)
                 for (int c = c0; c < c1; ++c) {
                     const ChirpRec &r = p->rec_host[c];
                     const double dx = ((double)r.p_hi.x + r.p_lo.x) - T[0], dy = ((double)r.p_hi.y + r.p_lo.y) - T[1],
                                  dz = ((double)r.p_hi.z + r.p_lo.z) - T[2];
                     const double n = std::sqrt(dx * dx + dy * dy + dz * dz);
                     const double fd = -two_over_lambda * (r.vel.x * dx + r.vel.y * dy + r.vel.z * dz) / n;
-                    live += std::fabs(fd - (double)r.p_hi.w) <= half_bw ? 1 : 0;
+                    const double off = std::fabs(fd - (double)r.p_hi.w);
+                    live += off <= half_bw ? 1 : 0;
+                    if (narrow) {
+                        const double vn = std::sqrt((double)r.vel.x * r.vel.x + (double)r.vel.y * r.vel.y +
+                                                    (double)r.vel.z * r.vel.z);
+                        const double chord = rho < n ? 2.0 * std::sin(0.5 * std::asin(rho / n)) : 2.0;
+                        const double bound = 1.05 * two_over_lambda * vn * chord +
+                                             1e-4 * (std::fabs(fd) + std::fabs((double)r.p_hi.w) + half_bw) + 1e-6;
+                        // dead for the whole tile only when provably so (NaN: kept)
+                        if (!(off > half_bw + bound)) {
+                            lo = std::min(lo, c);
+                            hi = c + 1;
+                        }
+                    }
                 }
                 // a live chirp costs its samples' MACs and the set-up, a dead one the vote
                 cost[(size_t)t * groups + g] = (double)live * (p->s_pad + 64) + (double)(c1 - c0 - live) * 24.0;
+                if (narrow && !(lo == c0 && hi == c1))
+                    span[(size_t)t * groups + g] = lo < hi ? kUnitSpan | ((lo - c0) << 15) | (hi - c0) : kUnitSpan;
             }
         }
     });
+    long long visited = 0;
+    for (FocusUnit &u : p->units_host) {
+        u.span = span[(size_t)u.tile * groups + u.group];
+        const int c0 = u.group * cpg, n = std::min(C, c0 + cpg) - c0;
+        visited += u.span ? std::max(0, (u.span & 0x7fff) - ((u.span >> 15) & 0x7fff)) : n;
+    }
+    p->span_permille = (int)std::lround(1000.0 * (double)visited / ((double)n_tiles * C));
     std::stable_sort(p->units_host.begin(), p->units_host.end(), [&](const FocusUnit &a, const FocusUnit &b) {
         return cost[(size_t)a.tile * groups + a.group] > cost[(size_t)b.tile * groups + b.group];
     });
@@ -1150,7 +1208,12 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         p->units_host.reserve((size_t)(n_tiles * p->plan_groups));
         for (long long t = 0; t < n_tiles; ++t)
             for (int g = 0; g < p->plan_groups; ++g) p->units_host.push_back(FocusUnit{0, (int)t, g, 0});
-        if (path != TDC_PATH_FP64_PHASE && path != TDC_PATH_GENERAL_FP64) order_units_by_cost(p, tile_cols);
+        // (only the whole-row FP32-bulk focus reads unit spans, and not when it keeps its
+        // per-chirp sums: those would be left unwritten for the skipped chirps)
+        p->span_permille = 1000;
+        if (path != TDC_PATH_FP64_PHASE && path != TDC_PATH_GENERAL_FP64)
+            order_units_by_cost(p, tile_cols,
+                                path == TDC_PATH_FP32_BULK && !seg && !p->keep_sums && !p->offsets_applied);
         p->plan_path = path;
         p->plan_P = P;
         p->plan_C = C;
@@ -1293,6 +1356,7 @@ int focus_resident(tdc_processor *p, float2 *image_dev, cudaStream_t st, int &la
     p->stats.general_variant = path == TDC_PATH_GENERAL ? plan.variant : 0;
     p->stats.tile_cols = job.tile_cols;
     p->stats.motion_segment = path == TDC_PATH_FP32_MOTION ? job.seg_len : 0;
+    p->stats.span_permille = path == TDC_PATH_FP32_BULK && !plan.seg && !store ? p->span_permille : 1000;
     p->stats.anchor_pixels = 0;
     if (path == TDC_PATH_FP32_BULK && !plan.seg && plan.anchored && !store && !std::isfinite(job.half_bw) &&
         job.tile_cols == 0)
@@ -1685,6 +1749,10 @@ int tdc_processor_set_chirp_offsets_device(tdc_processor *p, const double *offse
                                   static_cast<cudaStream_t>(stream)),
            "chirp positions kernel");
     ++p->state_epoch;
+    if (offsets_dev && !p->offsets_applied) {
+        p->offsets_applied = true;
+        p->plan_path = -1;  // replan without unit spans
+    }
     return TDC_OK;
 }
 

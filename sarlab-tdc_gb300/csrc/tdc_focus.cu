@@ -269,10 +269,16 @@ __device__ __forceinline__ void focus_fp32_body(const FocusJob *__restrict__ job
         __syncthreads();
 
         const int C = sJ.C;
-        const int c0 = un.group * sJ.chirps_per_group;
-        const int c1 = min(C, c0 + sJ.chirps_per_group);
+        int c0 = un.group * sJ.chirps_per_group;
+        int c1 = min(C, c0 + sJ.chirps_per_group);
+        if (!STORE && un.span) {
+            // the chirps of the group that the tile may see in band (the rest are out of band
+            // for all its pixels; the storing instance writes every chirp's sum, so it takes all)
+            c1 = min(c1, c0 + (un.span & 0x7fff));
+            c0 += (un.span >> 15) & 0x7fff;
+        }
         const int CB = sJ.stage_chirps;
-        const int nblk = (c1 - c0 + CB - 1) / CB;
+        const int nblk = c1 > c0 ? (c1 - c0 + CB - 1) / CB : 0;
         const int s_pad = sJ.s_pad;
         const uint32_t row_bytes = static_cast<uint32_t>(s_pad) * 8u;
         const float4 *__restrict__ xw = sJ.xw;

@@ -156,8 +156,10 @@ struct FocusUnit {
     int job;
     int tile;
     int group;
-    int pad_;
+    int span;  // 0: the group's chirps; else kUnitSpan | lo << 15 | hi: the chirps group x cpg + [lo, hi)
+               // (the FP32-bulk kernels; the host sets it only for chirps the tile cannot see in band)
 };
+constexpr int kUnitSpan = 1 << 30;
 
 // Kernel-side status bits (written to the status word in scratch).
 enum StatusBits : int {

@@ -194,6 +194,12 @@ struct tdc_processor {
     tdc::impl::DevBuf grid_stage, grid_hi, grid_lo;
     // Centre pixel (x, y, z) of each work tile, flat tiles and block tiles.
     std::vector<double> tile_centre_flat, tile_centre_block;
+    // Largest distance from each tile's centre pixel to its other pixels (flat, block tiles).
+    std::vector<double> tile_radius_flat, tile_radius_block;
+    // Chirp offsets applied on the device since the last prepare (rec_host's positions are then
+    // not the ones the kernels use: no unit spans from them).
+    bool offsets_applied = false;
+    int span_permille = 1000;  // chirps the planned units visit, per mille of tiles x chirps
     // Host copy of the chirp records (sample 0), for the planner's cost estimate.
     std::vector<tdc::ChirpRec> rec_host;
 

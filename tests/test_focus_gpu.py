@@ -603,3 +603,50 @@ def test_block_tiles_follow_a_new_grid_of_the_same_size(cuda_device):
         assert p.lastStats()["tile_cols"] == 16
         ref = _oracle(api, grid, args).reshape(img.shape)
         _check(img, ref, l2=2e-4, phase=None)
+
+
+def test_unit_spans_skip_only_chirps_out_of_band_for_the_whole_tile(cuda_device):
+    """Under a finite band each work unit visits only the chirps that some pixel of its tile can
+    see in band (span_permille < 1000). The skipped chirps are out of band for every pixel, so
+    the image is bit for bit the one without spans (chirp offsets of zero turn them off) and
+    matches the oracle. A grid of the same shape moved along the rail gets spans of its own."""
+    import torch
+
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=95, n_pri=600, n_samples=128, nx=64, ny=48, rail_len=0.6, device="cuda")
+    api = _moving_api(sc, speed=0.08)
+    args = (0.0, 14.0, False, True, True)
+    grid = sc.grid.astype(np.float32)
+
+    def focus(offsets):
+        p = _sarlabtdc.TdcProcessor(0)
+        p.setRawData(*api.values())
+        p.setFocusGrid(grid)
+        p.prepare(*args)
+        p.uploadGrid()
+        if offsets:
+            p.setChirpOffsetsDevice(torch.zeros((sc.n_pri, 3), dtype=torch.float64, device="cuda"))
+        img = torch.empty(p.numPixels(), dtype=torch.complex64, device="cuda")
+        p.focusDevice(img)
+        p.check()
+        return img.cpu().numpy(), p.lastStats()
+
+    img, st = focus(False)
+    img0, st0 = focus(True)
+    assert st["tile_cols"] == 16 and st["span_permille"] < 700, st["span_permille"]
+    assert st0["span_permille"] == 1000
+    np.testing.assert_array_equal(img, img0)
+    ref = _oracle(api, grid, args)
+    _check(img, ref, l2=2e-4, phase=None)
+    # the same processor, a grid of the same shape 0.1 m further along the rail
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setFocusGrid(grid)
+    p.start(*args)
+    moved = grid.copy()
+    moved[..., 0] += 0.1
+    p.setFocusGrid(moved)
+    p.start(*args)
+    assert p.lastStats()["span_permille"] < 1000
+    _check(p.getFocusedImage(), _oracle(api, moved, args).reshape(moved.shape[:2]), l2=2e-4, phase=None)
