@@ -23,6 +23,11 @@
 // Chirp sample rows and trajectory records are staged global->shared with
 // cp.async.bulk on an mbarrier pipeline (kFocusStages deep) and read back as
 // broadcast 128-bit shared loads shared by all 512 pixels of the tile.
+//
+// Two variations planned by the host: focus_fp32_anchored_kernel forms the range in
+// double-float once per 32 pixels and chirp and each pixel's difference from it in FP32
+// (short rows, unbounded band); under a finite band a work unit may cover only the chirps
+// of its group that its tile can see in band (FocusUnit::span).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -73,10 +78,10 @@ struct SharedPixel {
 // needs only its range difference dR = R - R0 = d.(d - 2e) / (R0 + R) in FP32 (d = pixel -
 // anchor, e = antenna - anchor: no cancellation, |dR| <= |d|) and small corrections
 // alpha0 + g0 dR, beta0 + g1 dR, QL0 e^{j 2 pi L g1 dR} (|2 pi L g1 dR| <= 0.25 by the host's
-// bound). With an unbounded band and finite
-// velocities and window centres, a chirp's window weight is 1 (0 where the antenna sits on the
-// pixel: NaN Doppler), so this instance forms no Doppler frequency. Its chirp sums q0 H go
-// into a per-stage sum by complex FMA, and the stage sums into the Kahan-compensated sum.
+// bound). With an unbounded band and finite velocities and window centres, a chirp's window
+// weight is 1 (0 where the antenna sits on the pixel: NaN Doppler), so this instance forms no
+// Doppler frequency. Its chirp sums q0 H go into a per-stage sum by complex FMA, and the stage
+// sums into the Kahan-compensated sum.
 constexpr int kAnchorRecs = kFocusPT * kAnchorMaxStageChirps;  // anchor records per warp and stage
 struct SharedAnchor {
     float4 d[kFocusPT][kFocusThreads];              // pixel - anchor per slot (x, y, z, 0)
