@@ -49,3 +49,23 @@ def test_blocks_assemble_the_whole_grid_bit_for_bit(cuda_device, world):
     np.testing.assert_array_equal(_focus_blocks(sc, api, world, pin=True), whole)
     # planned per block, the chirp groups (each pixel's summation order) may differ: FP32 rounding
     assert rel_l2(_focus_blocks(sc, api, world, pin=False), whole) < 1e-6
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_anchored_blocks_assemble_the_whole_grid_bit_for_bit(cuda_device, world):
+    """With anchored ranges (32 consecutive pixels share an anchor) on a grid of 40 columns:
+    the blocks start on multiples of 32 pixels (4 rows), so every pixel keeps its anchor and
+    the assembled image equals the whole grid's bit for bit."""
+    import _sarlabtdc
+
+    sc = scenes.small_scene(seed=302, n_pri=512, n_samples=256, nx=40, ny=57, jitter=0.2e-3, spacing=1e-3,
+                            device="cuda")
+    api = sc.api_arrays()
+    p = _sarlabtdc.TdcProcessor(0)
+    p.setRawData(*api.values())
+    p.setFocusGrid(sc.grid.astype(np.float32))
+    p.start(*START)
+    assert p.lastStats()["anchor_pixels"] == 32
+    whole = p.getFocusedImage()
+    assert sharding.row_align(40) == 4
+    np.testing.assert_array_equal(_focus_blocks(sc, api, world, pin=True), whole)
