@@ -86,10 +86,15 @@ struct Batch {
 constexpr size_t kBatchOffJobs = 256;
 constexpr int kMaxBatchJobs = 64;
 
-// Correlations per work unit in the request loop: one launch of ~1e12 correlations
-// (~130 ms) holds at least two units per resident CTA.
+// Correlations per work unit in the request loop, and per launch: ~5e11 correlations
+// (~65 ms) with at least two units per resident CTA. (On the config-4 mix, launches of 5e11
+// gave p50 8.1-8.2 s against 8.5-8.8 s with 1e12, 8.7 s with 2.5e11 and 10.3 s with 2e12, at
+// the same p99 and throughput.)
 constexpr double kServerUnitWork = 1.0e9;
-constexpr double kServerBatchWork = 1.0e12;
+#ifndef TDC_SERVER_BATCH_WORK
+#define TDC_SERVER_BATCH_WORK 5.0e11
+#endif
+constexpr double kServerBatchWork = TDC_SERVER_BATCH_WORK;
 // Priority: shortest estimated remaining service first, aged so that waiting jobs
 // are not starved (a job gains kAging seconds of priority per second it waits).
 constexpr double kRateEstimate = 7.0e12;  // correlations per second
