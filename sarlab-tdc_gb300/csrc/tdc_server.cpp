@@ -96,9 +96,15 @@ constexpr double kServerUnitWork = 1.0e9;
 #endif
 constexpr double kServerBatchWork = TDC_SERVER_BATCH_WORK;
 // Priority: shortest estimated remaining service first, aged so that waiting jobs
-// are not starved (a job gains kAging seconds of priority per second it waits).
+// are not starved (a job gains kAging seconds of priority per second it waits). On the
+// config-4 mix (Poisson 20/s, 3.3x the GPU's rate): aging 0.05 gave p50 0.53 s and p99 27.9 s,
+// 0.02 0.40 / 28.1 s, 0.1 1.7-2.2 / 27.8-28.1 s, 0.25 6.4 / 29.1-29.3 s, 0.5 8.5 / 29.1 s, 1.0
+// 11.7 / 29.1 s, at 7,790-7,870 Gcorr/s throughout.
 constexpr double kRateEstimate = 7.0e12;  // correlations per second
-constexpr double kAging = 0.5;
+#ifndef TDC_SERVER_AGING
+#define TDC_SERVER_AGING 0.05
+#endif
+constexpr double kAging = TDC_SERVER_AGING;
 
 // The kernel a job's units run in: jobs share a launch only with jobs of the same kind (the
 // same kernel instance, so a job's arithmetic does not depend on the jobs beside it). -1: not
