@@ -642,13 +642,32 @@ def serving_leg(args):
               "launches": st["launches"]}
     log(f"request loop: {served}")
 
-    # serial: the same jobs one at a time (each alone on the GPU), FIFO on the same arrivals
+    # serial: the same jobs one after another through the processor (tdc_processor_start: each
+    # job's whole focus in one launch, its image copied out), FIFO on the same arrivals
+    import ctypes
+
+    import _sarlabtdc
+    import _tdc_capi as L
+
+    lib = L.lib()
+    proc = _sarlabtdc.TdcProcessor(0)
+    bore = np.array([0.0, 1.0, 0.0], np.float32)
     service = []
-    with FocusServer(max_jobs=1) as one:
-        for j in jobs:
-            t = time.perf_counter()
-            one.wait(one.submit(j["raw"], j["st"], j["pos"], j["grid"], j["K"], j["f0"], start=start))
-            service.append(time.perf_counter() - t)
+    for j in jobs:
+        t = time.perf_counter()
+        n_pri, n_s = j["raw"].shape
+        rows, cols = j["grid"].shape[:2]
+        # per-chirp positions: the per-sample arrays of setRawData are replaced by the trajectory
+        L.check(lib.tdc_processor_set_raw_data(proc._h, L.ptr(j["raw"]), None, L.ptr(j["st"]), L.ptr(j["pos"]), None,
+                                               None, n_pri, n_s, float(j["K"]), float(j["f0"]), L.ptr(bore)))
+        L.check(lib.tdc_processor_set_trajectory_per_chirp(proc._h, L.ptr(j["pos"]), None, None))
+        L.check(lib.tdc_processor_set_focus_grid(proc._h, L.ptr(j["grid"]), rows, cols))
+        L.check(lib.tdc_processor_start(proc._h, *start[:2], int(start[2]), int(start[3]), int(start[4])))
+        buf = lib.tdc_processor_image_buffer(proc._h)
+        img = np.empty(rows * cols, np.complex64)
+        ctypes.memmove(img.ctypes.data, buf, img.nbytes)
+        service.append(time.perf_counter() - t)
+    del proc
     finish, lat_s = 0.0, []
     for a, sv in zip(arrivals, service):
         finish = max(finish, a) + sv
@@ -662,8 +681,9 @@ def serving_leg(args):
                         "256..8192 chirps (log-uniform), 256/512/1024 samples, 1-100 targets",
             "unit": UNIT, "total_correlations": total, "request_loop": served, "serial_processor": serial,
             "offered_gcorr_s": round(total / (arrivals[-1] - arrivals[0]) / 1e9, 1),
-            "serial_how": "the same jobs one at a time through a one-slot request loop, FIFO on the same arrivals "
-                          "(latency = queueing on those arrivals + measured service time)",
+            "serial_how": "the same jobs one after another through the processor (tdc_processor_start, each "
+                          "job's focus in one launch), FIFO on the same arrivals (latency = queueing on those "
+                          "arrivals + measured service time)",
             "clocks": clk}
 
 
