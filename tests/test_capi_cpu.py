@@ -200,9 +200,9 @@ def test_device_buffers_are_checked_before_any_kernel_writes_them():
 
 def test_kernels_compile_without_register_spills(engine_lib):
     """ptxas resource report of the build (sarlab-tdc_gb300/_build/ptxas.log): every
-    focus, adjoint and general-kernel instance fits its registers (no spill stores or
-    loads, <= 168 registers for 3 CTAs of 128 threads), so a change that pushes a hot
-    loop into local memory fails here, before it reaches a GPU."""
+    focus (including the anchored-range kernel), adjoint and general-kernel instance fits
+    its registers (no spill stores or loads, <= 168 registers for 3 CTAs of 128 threads), so
+    a change that pushes a hot loop into local memory fails here, before it reaches a GPU."""
     import re
 
     log = (ROOT / "sarlab-tdc_gb300" / "_build" / "ptxas.log").read_text()
@@ -217,8 +217,9 @@ def test_kernels_compile_without_register_spills(engine_lib):
     hot = {n: v for n, v in seen.items()
            if any(k in n for k in ("focus_fp32", "focus_general", "focus_motion", "adjoint_fp32_kernel",
                                    "focus_fp64"))}
-    # 4 bulk + 2 segmented + 7 general + 2 smooth-motion + 2 FP64 + 2 adjoint instances
-    assert len(hot) >= 19, sorted(hot)
+    # 4 bulk + 1 anchored + 2 segmented + 7 general + 2 smooth-motion + 2 FP64 + 2 adjoint instances
+    assert len(hot) >= 20, sorted(hot)
+    assert any("focus_fp32_anchored_kernel" in n for n in hot)
     for name, (st, ld, regs) in hot.items():
         assert st == 0 and ld == 0, f"{name}: {st} B spill stores, {ld} B spill loads"
         assert regs <= 168 or "focus_fp64" in name, f"{name}: {regs} registers"
