@@ -35,6 +35,14 @@ def test_library_builds_and_exports_every_declared_symbol(engine_lib):
     assert engine_lib.tdc_abi_version() == 1
 
 
+def test_c_abi_header_compiles_as_c99():
+    """include/tdc_gb300.h is a C header (what a cgo / JNI / ctypes binding includes): it must
+    compile as plain C99, not only as C++."""
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c",
+                        str(ROOT / "include" / "tdc_gb300.h")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_binding_signatures_cover_the_header():
     import _tdc_capi
 
