@@ -370,8 +370,11 @@ int tdc_selftest_wait_timeout(int device, int limit_us, int *timed_out, double *
  * chains that provision all device memory once at start-up (real-time or
  * certified radar pipelines with a fixed budget), plug-ins inside a host
  * framework that owns the device allocator, code that must not call cudaMalloc
- * during stream capture. tdc_focus_noalloc runs the same FP32-bulk focus as
- * tdc_processor_focus_device on inputs and an output the caller owns; its
+ * during stream capture. tdc_focus_noalloc runs the FP32-bulk focus of
+ * tdc_processor_focus_device, with every (pixel, chirp) range in double-float and
+ * every work unit over its whole chirp group (the anchored ranges and unit spans
+ * the processor plans from its host copies of the grid and trajectory are not
+ * taken), on inputs and an output the caller owns; its
  * scratch memory is a fixed array inside this library (TDC_NOALLOC_SCRATCH_BYTES
  * on every GPU that loads the library, held until the process exits), so it
  * calls no cudaMalloc / cudaFree. That limits the grid to about 2M pixels, and
