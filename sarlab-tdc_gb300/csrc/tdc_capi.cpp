@@ -870,7 +870,7 @@ int choose_tile_cols(const tdc_processor *p)
 // A chirp outside the span is out of band for every pixel of the tile (with a 5% margin on
 // that bound and 1e-4 relative for the kernel's FP32 arithmetic), so the zero-window
 // instance would skip it for every warp: skipping it in the unit changes no sum.
-void order_units_by_cost(tdc_processor *p, int tile_cols, bool narrow)
+void plan_unit_order_and_spans(tdc_processor *p, int tile_cols, bool narrow)
 {
     if (!std::isfinite(p->opts.bw) || p->rec_host.size() != (size_t)p->C || p->units_host.size() < 2) return;
     const std::vector<double> &centres = tile_cols ? p->tile_centre_block : p->tile_centre_flat;
@@ -878,7 +878,7 @@ void order_units_by_cost(tdc_processor *p, int tile_cols, bool narrow)
     const long long n_tiles = (long long)centres.size() / 3;
     const int C = p->C, cpg = p->plan_cpg, groups = p->plan_groups;
     if ((long long)p->units_host.size() != n_tiles * groups) return;
-    narrow = narrow && (long long)radii.size() == n_tiles && cpg < (1 << 15);
+    narrow = narrow && (long long)radii.size() == n_tiles && cpg < kUnitSpanMax;
     const double two_over_lambda = (double)(2.0f / p->lambda), half_bw = (double)(p->opts.bw / 2.0f);
     std::vector<double> cost((size_t)n_tiles * groups, 0.0);
     std::vector<int> span((size_t)n_tiles * groups, 0);
@@ -914,7 +914,7 @@ void order_units_by_cost(tdc_processor *p, int tile_cols, bool narrow)
                 // a live chirp costs its samples' MACs and the set-up, a dead one the vote
                 cost[(size_t)t * groups + g] = (double)live * (p->s_pad + 64) + (double)(c1 - c0 - live) * 24.0;
                 if (narrow && !(lo == c0 && hi == c1))
-                    span[(size_t)t * groups + g] = lo < hi ? kUnitSpan | ((lo - c0) << 15) | (hi - c0) : kUnitSpan;
+                    span[(size_t)t * groups + g] = lo < hi ? unit_span(lo - c0, hi - c0) : unit_span(0, 0);
             }
         }
     });
@@ -922,7 +922,7 @@ void order_units_by_cost(tdc_processor *p, int tile_cols, bool narrow)
     for (FocusUnit &u : p->units_host) {
         u.span = span[(size_t)u.tile * groups + u.group];
         const int c0 = u.group * cpg, n = std::min(C, c0 + cpg) - c0;
-        visited += u.span ? std::max(0, (u.span & 0x7fff) - ((u.span >> 15) & 0x7fff)) : n;
+        visited += u.span ? std::max(0, unit_span_hi(u.span) - unit_span_lo(u.span)) : n;
     }
     p->span_permille = (int)std::lround(1000.0 * (double)visited / ((double)n_tiles * C));
     std::stable_sort(p->units_host.begin(), p->units_host.end(), [&](const FocusUnit &a, const FocusUnit &b) {
@@ -1212,7 +1212,7 @@ int focus_plan(tdc_processor *p, FocusPlan &plan, double max_unit_work)
         // per-chirp sums: those would be left unwritten for the skipped chirps)
         p->span_permille = 1000;
         if (path != TDC_PATH_FP64_PHASE && path != TDC_PATH_GENERAL_FP64)
-            order_units_by_cost(p, tile_cols,
+            plan_unit_order_and_spans(p, tile_cols,
                                 path == TDC_PATH_FP32_BULK && !seg && !p->keep_sums && !p->offsets_applied);
         p->plan_path = path;
         p->plan_P = P;

@@ -279,8 +279,8 @@ __device__ __forceinline__ void focus_fp32_body(const FocusJob *__restrict__ job
         if (!STORE && un.span) {
             // the chirps of the group that the tile may see in band (the rest are out of band
             // for all its pixels; the storing instance writes every chirp's sum, so it takes all)
-            c1 = min(c1, c0 + (un.span & 0x7fff));
-            c0 += (un.span >> 15) & 0x7fff;
+            c1 = min(c1, c0 + unit_span_hi(un.span));
+            c0 += unit_span_lo(un.span);
         }
         const int CB = sJ.stage_chirps;
         const int nblk = c1 > c0 ? (c1 - c0 + CB - 1) / CB : 0;

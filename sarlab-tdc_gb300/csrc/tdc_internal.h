@@ -156,10 +156,15 @@ struct FocusUnit {
     int job;
     int tile;
     int group;
-    int span;  // 0: the group's chirps; else kUnitSpan | lo << 15 | hi: the chirps group x cpg + [lo, hi)
+    int span;  // 0: the group's chirps; else unit_span(lo, hi): the chirps group x cpg + [lo, hi)
                // (the FP32-bulk kernels; the host sets it only for chirps the tile cannot see in band)
 };
-constexpr int kUnitSpan = 1 << 30;
+// FocusUnit::span: a marker bit and two 15-bit chirp offsets within the group (groups of
+// fewer than kUnitSpanMax chirps).
+constexpr int kUnitSpanMax = 1 << 15;
+__host__ __device__ constexpr int unit_span(int lo, int hi) { return (1 << 30) | (lo << 15) | hi; }
+__host__ __device__ constexpr int unit_span_lo(int span) { return (span >> 15) & (kUnitSpanMax - 1); }
+__host__ __device__ constexpr int unit_span_hi(int span) { return span & (kUnitSpanMax - 1); }
 
 // Kernel-side status bits (written to the status word in scratch).
 enum StatusBits : int {
