@@ -194,9 +194,10 @@ int tdc_processor_set_motion_path(tdc_processor *proc, int enable);
  * range and phase terms are formed in double-float once per chirp; each pixel adds its range
  * difference from the anchor in FP32 (exact in form: d.(d - 2e) / (R0 + R), no cancellation).
  * Taken only when no pixel lies farther than 5 cm from its anchor (grids whose rows are a
- * multiple of 32 pixels, or narrower than 5 cm, at up to 3 mm spacing), which keeps the phase
- * within about 2e-5 rad of the per-pixel double-float range's. Off: every (pixel, chirp) range
- * in double-float. Extension without a reference counterpart; takes effect at the next focus. */
+ * multiple of 32 pixels, or narrower than 5 cm, at up to 3 mm spacing), which keeps each
+ * (pixel, chirp) phase within about 3e-5 rad of the per-pixel double-float range's at 77 GHz
+ * (1e-5 rad on 1 mm grids). Off: every (pixel, chirp) range in double-float. Extension without
+ * a reference counterpart; takes effect at the next focus. */
 int tdc_processor_set_anchored_ranges(tdc_processor *proc, int enable);
 
 /*

@@ -31,7 +31,8 @@ constexpr int kFocusStageTarget = TDC_FOCUS_STAGE_TARGET;  // bytes of chirp row
 // Anchored ranges of the FP32-bulk kernel (pixels of a warp share a double-float anchor
 // range per chirp, each adds its FP32 range difference): at most this many chirps per stage,
 // and no pixel farther than kAnchorMaxDistance from its anchor. At 5 cm the FP32 range
-// difference keeps the phase within ~2e-5 rad of the double-float range's at 77 GHz.
+// difference keeps the phase within ~3e-5 rad of the double-float range's at 77 GHz (1e-5 at
+// the 1.6 cm of a 1 mm grid; tests/test_anchor_error_cpu.py).
 constexpr int kAnchorMaxStageChirps = 16;
 constexpr double kAnchorMaxDistance = 0.05;  // metres
 // Fewest work units per CTA slot the planner aims for where the grid and chirps allow
